@@ -1,0 +1,369 @@
+"""Throughput benchmark of the optimized-convolution Barnes interpolation.
+
+Workload (the headline configuration): a batch of B independent 2D fields,
+each 4096 x 2048 grid points (x, y) over the European domain (x0 = (-26, 34.5),
+step = 75/4096 x 37.5/2048 degrees), N = 100k uniformly placed samples with
+values 1000 + 20 sin(lon/10) cos(lat/8) + N(0, 2^2), sigma = 1 degree,
+num_iter = 4, max_dist = 3.5; float32-compensated form (fp32c).  Seeded
+synthetic data stand in for observations.
+
+Metric: Mgridpts/s = batch grid points x steps / time.  `value` runs the
+device entry point with inputs resident in HBM; `e2e` runs the C-ABI host
+entry (fb_interpolate_host) from pinned host buffers, copies included.  The
+plain float64 form of the same batch, its error against the float64 result
+and the CPU oracle (the reference's algorithm restated in C) are reported
+beside it.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--batch B]
+                       [--precision fp32c|fp64] [--impl gpu|reference]
+For N > 1 (torchrun) every rank runs its own batch (replicas: the fields are
+independent, no collective on the data path); rank 0 prints the JSON line.
+"""
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "fast-barnes-py_gb300"))
+sys.path.insert(0, ROOT)
+
+W, H, NPTS, SIGMA, NITER, MAX_DIST = 4096, 2048, 100_000, 1.0, 4, 3.5
+X0 = (-26.0, 34.5)
+STEP = (75.0 / W, 37.5 / H)
+METRIC = "Mgridpts/s 2D n=4: fp32-compensated batched vs plain fp64 on GB300 at fixed error"
+
+
+def field_inputs(seed):
+    rng = np.random.default_rng(seed)
+    lon = rng.uniform(-26, 49, NPTS)
+    lat = rng.uniform(34.5, 72, NPTS)
+    val = 1000 + 20 * np.sin(lon / 10) * np.cos(lat / 8) + rng.normal(0, 2, NPTS)
+    return np.ascontiguousarray(np.c_[lon, lat]), val
+
+
+def workload_config(batch, precision):
+    return {"workload": f"2D {W}x{H} grid, N={NPTS} samples per field, sigma=1 deg, n={NITER}, "
+                        f"batch of {batch} fields ({precision})",
+            "grid": [W, H], "n_samples": NPTS, "sigma_deg": SIGMA, "num_iter": NITER, "batch_fields": batch,
+            "precision": precision,
+            "l2": "inputs larger than L2: each step touches ~%d MB of distinct field outputs" % (batch * W * H * 4 >> 20)}
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the timed region runs."""
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, x):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_oracle_rate(nthreads, seconds=12.0, max_fields=3):
+    """The reference's algorithm (the C oracle) on this host: Mgridpts/s."""
+    from oracle import oracle
+    oracle.build()
+    done, t_total = 0, 0.0
+    pts, val = field_inputs(1000)
+    while done < max_fields and t_total < seconds:
+        t0 = time.perf_counter()
+        oracle.interpolate(pts, val, SIGMA, X0, STEP, (W, H), NITER, MAX_DIST, nthreads=nthreads)
+        t_total += time.perf_counter() - t0
+        done += 1
+    return W * H * done / t_total / 1e6, done, t_total
+
+
+def run_reference(args, world, rank):
+    """--impl reference: the reference's CPU algorithm (oracle port) with all
+    host threads, one field per step."""
+    if rank != 0:
+        return
+    from oracle import oracle
+    oracle.build()
+    nth = os.cpu_count() or 1
+    pts, val = field_inputs(1000)
+    for _ in range(args.warmup):
+        oracle.interpolate(pts, val, SIGMA, X0, STEP, (W, H), NITER, MAX_DIST, nthreads=nth)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.interpolate(pts, val, SIGMA, X0, STEP, (W, H), NITER, MAX_DIST, nthreads=nth)
+    dt = time.perf_counter() - t0
+    value = W * H * args.steps / dt / 1e6
+    sample = f"{args.steps} fields of {W}x{H}, N={NPTS}, float64, one field per step"
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mgridpts/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)", "config": workload_config(1, "fp64"),
+            "cpu_baseline": {"value": value, "unit": "Mgridpts/s", "cores": nth, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "Mgridpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=8)
+    ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist_setup()
+
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+
+    import torch
+    from fastbarnes_gb300 import _lib
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    L = _lib.lib()
+    prec = _lib.PRECISIONS[args.precision]
+    B = args.batch
+
+    # device-resident inputs, one output per field
+    fields = [field_inputs(1000 + 97 * rank + f) for f in range(B)]
+    d_pts = [torch.as_tensor(p, device=dev) for p, _ in fields]
+    d_val = [torch.as_tensor(v, device=dev) for _, v in fields]
+    outs = [torch.empty((H, W), dtype=torch.float32, device=dev) for _ in range(B)]
+    d = _lib.dvec
+    c_sigma, c_x0, c_step = d([SIGMA, SIGMA]), d(list(X0)), d(list(STEP))
+    c_size = d([W, H], ctypes.c_int64)
+    mdw = math.exp(-MAX_DIST ** 2 / 2)
+    need = ctypes.c_size_t(0)
+
+    def ws_for(pc):
+        _lib.check(L.fb_workspace_size(0, pc, 2, NPTS, c_sigma, c_step, c_size, NITER, ctypes.byref(need)))
+        return torch.empty(need.value, dtype=torch.uint8, device=dev)
+
+    ws = ws_for(prec)
+    stream = torch.cuda.current_stream(dev)
+    sptr = ctypes.c_void_p(stream.cuda_stream)
+
+    def step(pc=prec, wsb=ws, out_list=outs, out_f64=0):
+        for f in range(B):
+            rc = L.fb_interpolate(0, pc, 2, d_pts[f].data_ptr(), d_val[f].data_ptr(), NPTS, c_sigma, c_x0, c_step,
+                                  c_size, NITER, mdw, out_list[f].data_ptr(), out_f64, wsb.data_ptr(), wsb.numel(),
+                                  sptr)
+            if rc != 0:
+                _lib.check(rc, "fb_interpolate")
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    # ---- timed region: device entry, inputs resident in HBM --------------
+    _lib.check(L.fb_profile_begin())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier(world)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+    t_ms = ev0.elapsed_time(ev1)
+    maxrec = 64 * args.steps * B
+    stages = (ctypes.c_int * maxrec)()
+    times = (ctypes.c_float * maxrec)()
+    nrec = ctypes.c_int(0)
+    _lib.check(L.fb_profile_end(stages, times, maxrec, ctypes.byref(nrec)))
+    t_ms = max_over_ranks(world, t_ms)
+    gridpts = W * H * B * args.steps * world
+    value = gridpts / (t_ms / 1e3) / 1e6
+
+    # per-stage launch times -> roofline of the dominant kernel
+    per_stage = {}
+    for i in range(nrec.value):
+        per_stage.setdefault(stages[i], []).append(times[i])
+    sz = 4 if prec == _lib.FB_FP32C else 8
+    alg = {0: NPTS * (24 + 16 * 4),                          # sort: coords+value read, keys/idx passes
+           1: NPTS * 28 + W * H * 2 * sz,                    # splat + row passes: samples in, v,w out
+           2: W * H * 2 * sz + W * H * 4}                    # column passes + quotient: v,w in, float32 out
+    names = {0: "sample sort", 1: "k_axis x-passes (splat fused)", 2: "k_axis y-passes (quotient fused)"}
+    stage_ms = {k: sum(v) / len(v) for k, v in per_stage.items()}
+    dom = max((k for k in stage_ms if k != 0), key=lambda k: sum(per_stage[k]))
+    peak, peak_kind = measured_peak()
+    achieved = alg[dom] / (stage_ms[dom] / 1e3) / 1e9
+    pipeline_bytes = NPTS * 28 + W * H * (4 * sz + 4)
+    pipeline_gbs = pipeline_bytes * B * args.steps / (t_ms / 1e3) / 1e9
+
+    # ---- plain float64 form of the same batch + error at fixed config -----
+    ws64 = ws_for(_lib.FB_FP64) if prec != _lib.FB_FP64 else ws
+    outs64 = [torch.empty((H, W), dtype=torch.float64, device=dev) for _ in range(B)]
+    step(_lib.FB_FP64, ws64, outs64, 1)
+    torch.cuda.synchronize()
+    k64 = max(2, args.steps // 4)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(k64):
+        step(_lib.FB_FP64, ws64, outs64, 1)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    fp64_value = W * H * B * k64 / (e0.elapsed_time(e1) / 1e3) / 1e6
+    q32 = torch.empty((H, W), dtype=torch.float64, device=dev)
+    L.fb_interpolate(0, prec, 2, d_pts[0].data_ptr(), d_val[0].data_ptr(), NPTS, c_sigma, c_x0, c_step, c_size,
+                     NITER, mdw, q32.data_ptr(), 1, ws.data_ptr(), ws.numel(), sptr)
+    torch.cuda.synchronize()
+    a, b = q32.cpu().numpy(), outs64[0].cpu().numpy()
+    mm = ~np.isnan(a) & ~np.isnan(b)
+    err_rel = float(np.max(np.abs(a[mm] - b[mm])) / np.max(np.abs(b[mm])))
+    err_range = float(np.max(np.abs(a[mm] - b[mm])) / np.ptp(fields[0][1]))
+    mask_mismatch = int(np.sum(np.isnan(a) != np.isnan(b)))
+    del outs64, ws64
+
+    # ---- e2e: C-ABI host entry from pinned host memory --------------------
+    h_pts = [L.fb_host_alloc(NPTS * 16) for _ in range(B)]
+    h_val = [L.fb_host_alloc(NPTS * 8) for _ in range(B)]
+    h_out = [L.fb_host_alloc(W * H * 4) for _ in range(B)]
+    for f in range(B):
+        ctypes.memmove(h_pts[f], fields[f][0].ctypes.data, NPTS * 16)
+        ctypes.memmove(h_val[f], fields[f][1].ctypes.data, NPTS * 8)
+
+    def e2e_step():
+        for f in range(B):
+            rc = L.fb_interpolate_host(0, prec, 2, h_pts[f], h_val[f], NPTS, c_sigma, c_x0, c_step, c_size, NITER,
+                                       mdw, h_out[f], 0, sptr)
+            if rc != 0:
+                _lib.check(rc, "fb_interpolate_host")
+
+    for _ in range(2):
+        e2e_step()
+    k_e2e = max(2, args.steps // 4)
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(k_e2e):
+        e2e_step()
+    t_e2e = max_over_ranks(world, time.perf_counter() - t0)
+    e2e_value = W * H * B * k_e2e * world / t_e2e / 1e6
+    for p in h_pts + h_val + h_out:
+        L.fb_host_free(p)
+    L.fb_release()
+
+    # ---- CPU baseline (rank 0, N = 1 only) ----------------------------------
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        rate, nf, secs = cpu_oracle_rate(1)
+        cpu = {"value": rate, "unit": "Mgridpts/s", "cores": 1, "kind": "port",
+               "sample": f"{nf} field(s) of {W}x{H}, N={NPTS}, float64, single thread, {secs:.1f} s"}
+
+    launches_per_field = 0
+    # header init, bin keys, per radix pass (hist, scan, scatter), bin starts, two axis launches
+    radix_passes = (int(math.log2(H)) + 1 + 7) // 8
+    launches_per_field = 1 + 1 + 3 * radix_passes + 1 + 2
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "Mgridpts/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec == _lib.FB_FP32C else "f64",
+                "data": "synthetic (seeded uniform samples, smooth field + noise)",
+                "config": workload_config(B, args.precision) | {"parallelism": f"replicas x{world}"},
+                "gpu_launches": launches_per_field * B * args.steps,
+                "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
+                             "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                             "traffic": None, "algorithmic_bytes_per_launch": alg[dom],
+                             "launch_ms": stage_ms[dom],
+                             "stage_ms": {names[k]: v for k, v in stage_ms.items()},
+                             "pipeline_gbs": pipeline_gbs, "pipeline_frac": pipeline_gbs / peak},
+                "fp64_form": {"value": fp64_value, "unit": "Mgridpts/s", "speedup_of_fp32c": value / fp64_value},
+                "error_vs_fp64": {"rel_max": err_rel, "max_over_range": err_range, "mask_mismatch": mask_mismatch},
+                "e2e": {"value": e2e_value, "unit": "Mgridpts/s", "h2d_bytes_per_step": B * NPTS * 24,
+                        "d2h_bytes_per_step": B * W * H * 4, "entry": "fb_interpolate_host (pinned host buffers)"},
+                "cpu_baseline": cpu, "clocks": clk.summary()}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

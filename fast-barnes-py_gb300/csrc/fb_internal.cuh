@@ -1,0 +1,113 @@
+// fb_internal.cuh -- shared definitions of the GB300 fast-Barnes kernels.
+//
+// Data layout in HBM (one field):
+//   samples  : pts[N][dim] float64 (x fastest), val[N] float64 -- caller owned
+//   grid     : [z][y][x] row-major, x fastest, exactly the reference's
+//              size[::-1] layout (fastbarnes/interpolation.py:337-339)
+//   workspace: FieldHeader | bin keys | sort ping-pong | tile histograms |
+//              bin starts | two intermediate value/weight field pairs
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+namespace fbg {
+
+// Chunk length of the line-pass kernels: odd, so that 32 lanes holding
+// consecutive chunks of one line hit 32 different shared-memory banks.
+constexpr int K32 = 33;   // float32-compensated form
+constexpr int K64 = 17;   // float64 form (8-byte words: half-warp phases)
+
+constexpr int kMaxLineThreads = 1024;
+
+// Per-field scalars written on the device (min/max of the values, flags).
+struct FieldHeader {
+    unsigned long long vmin_key;   // ordered-integer encoding of min(val)
+    unsigned long long vmax_key;   // ordered-integer encoding of max(val)
+    int nan_seen;                  // any NaN in val -> offset is NaN
+    int error;                     // device-side error word (0 = ok)
+    int pad[2];
+};
+
+// Ordered encoding of a double so that unsigned integer order == numeric order.
+__host__ __device__ inline unsigned long long dbl_to_ordered(double x)
+{
+    unsigned long long u;
+#ifdef __CUDA_ARCH__
+    u = (unsigned long long)__double_as_longlong(x);
+#else
+    memcpy(&u, &x, 8);
+#endif
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+
+__host__ __device__ inline double ordered_to_dbl(unsigned long long k)
+{
+    unsigned long long u = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double((long long)u);
+#else
+    double x;
+    memcpy(&x, &u, 8);
+    return x;
+#endif
+}
+
+// offset = (min + max) / 2 as in _normalize_values (interpolation.py:204-212)
+__device__ inline double field_offset(const FieldHeader *h)
+{
+    if (h->nan_seen)
+        return __longlong_as_double(0x7ff8000000000000ll);
+    return (ordered_to_dbl(h->vmin_key) + ordered_to_dbl(h->vmax_key)) / 2.0;
+}
+
+// Geometry and parameters of one interpolation, shared by all kernels.
+struct Geometry {
+    int dim;
+    int64_t size[3];      // x, y, z extents (1 for missing axes)
+    double x0[3], step[3];
+    int T[3];             // half kernel size per axis
+    double alpha[3];      // tail value per axis (0 for the plain method)
+    int num_iter;
+    double thr;           // NaN mask level on the unscaled weight field
+};
+
+// Sorted-sample view handed to the splatting first-axis kernel.
+struct SampleView {
+    const double *pts;
+    const double *val;
+    int64_t npts;
+    const uint32_t *sorted_idx;   // sample indices ordered by bin (stable)
+    const uint32_t *bin_start;    // nbins + 1 offsets into sorted_idx
+    uint32_t nbins;
+    int bin_w;                    // 1D only: cells per bin
+    const FieldHeader *hdr;
+};
+
+// One launch of the line-pass kernel along one axis.
+struct AxisLaunch {
+    int axis;                 // 0 = x (contiguous lines), 1 = y, 2 = z
+    int64_t L;                // line length
+    int64_t elem_stride;      // distance between consecutive line elements
+    int64_t nlines;           // lines along this axis
+    int lines_per_cta;        // lines processed together (adjacent lines)
+    int64_t tile_len;         // output positions per tile (== L if untiled)
+    int64_t ntiles;           // tiles per line
+    int halo;                 // extra input cells on each side of a tile
+    int extent_max;           // largest smem extent of one line
+    int line_pitch;           // smem words (Real) reserved per line buffer
+    int chunks_pad;           // threads per line (chunks rounded up to 32)
+    int passes;               // box passes run in this launch
+    int T;
+    double alpha;
+    double inv_norm;          // 1/(2T+1+2alpha) for the scaled fp32 form, else 1
+    int fill_splat;           // 1: fill by splatting samples, 0: load from src
+    int store_quot;           // 1: last axis -> quotient + mask + offset
+    int out_f64;              // quotient output type: 1 = float64, 0 = float32
+    double thr;               // mask level in the units of the stored weights
+    const void *src_v, *src_w;
+    void *dst_v, *dst_w;
+    void *out;
+};
+
+}  // namespace fbg

@@ -1,0 +1,38 @@
+// fb_kernels.cuh -- host-side entry points of the kernel translation units.
+#pragma once
+#include "fb_internal.cuh"
+
+namespace fbg {
+
+// fb_sort.cu
+size_t sort_scratch_bytes(int64_t npts);
+cudaError_t sort_samples(const double *pts, const double *val, int64_t npts, const Geometry &g,
+                         int bin_w, uint32_t nbins, FieldHeader *hdr, uint32_t *scratch,
+                         uint32_t *bin_start, const uint32_t **sorted_idx, cudaStream_t st);
+
+// fb_axis.cu
+struct AxisPlanLimits {
+    int extent_max;      // longest line extent held in shared memory
+    size_t smem_limit;   // dynamic shared memory per block
+};
+AxisPlanLimits axis_limits(int precision);
+// Shared memory needed by one CTA of a launch.
+size_t axis_smem_bytes(int precision, const AxisLaunch &a);
+// Fills in lines_per_cta, extent_max, line_pitch, chunks_pad for a launch
+// whose L / tile_len / halo are set; returns false if it cannot be held.
+bool axis_shape(int precision, AxisLaunch &a);
+cudaError_t launch_axis(int precision, const AxisLaunch &a, const Geometry &g, const SampleView &sv,
+                        cudaStream_t st);
+// Standalone n-pass box filter over contiguous device lines (no splat, no
+// quotient): used for the reference's _accumulate_*_array entry points.
+cudaError_t launch_lines(int precision, void *data, int64_t nlines, int64_t len, int T, double alpha,
+                         int passes, int normalize, cudaStream_t st);
+
+// fb_s2.cu
+cudaError_t launch_lambert_to_map(const double *geo, double *map, int64_t n, const double *proj,
+                                  cudaStream_t st);
+cudaError_t launch_resample(const float *lam, int64_t lam_w, int64_t lam_h, const double *lam_x0,
+                            const double *x0, const double *step, const int64_t *size,
+                            const double *proj, float *out, double *tab, cudaStream_t st);
+
+}  // namespace fbg

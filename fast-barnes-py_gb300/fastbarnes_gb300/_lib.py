@@ -1,0 +1,124 @@
+"""ctypes binding of libfastbarnes_gb300.so (the C ABI in include/fastbarnes_gb300.h).
+
+The library is built in-tree (``build.py`` next to this package, or
+``__graft_entry__.build()`` at the repository root).  There is no CPU
+fallback: if the library or a CUDA device is missing, every entry point that
+needs them raises.
+"""
+import ctypes
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfastbarnes_gb300.so")
+
+FB_OK = 0
+FB_ERR_KERNEL_SIZE = 2
+FB_FP64, FB_FP32C = 0, 1
+FB_OPTIMIZED_CONVOLUTION, FB_CONVOLUTION = 0, 1
+
+PRECISIONS = {"fp64": FB_FP64, "float64": FB_FP64, "fp32c": FB_FP32C}
+
+_lib = None
+_lock = threading.Lock()
+
+
+class FastBarnesError(RuntimeError):
+    """A call into libfastbarnes_gb300 failed; the message is the library's."""
+
+
+def build(force=False):
+    """Compile the CUDA library for sm_103a (nvcc must be on PATH)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_fbg_build", os.path.join(os.path.dirname(HERE), "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(force=force)
+
+
+def lib():
+    """The loaded library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise FastBarnesError(
+                f"{LIB_PATH} is missing: build it with fast-barnes-py_gb300/build.py "
+                "(there is no CPU fallback)")
+        L = ctypes.CDLL(LIB_PATH)
+        P, d, i, i64, sz = ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int64, ctypes.c_size_t
+        sig = {
+            "fb_version": ([], ctypes.c_char_p),
+            "fb_last_error": ([], ctypes.c_char_p),
+            "fb_half_kernel_size_opt": ([d, d, i], i),
+            "fb_tail_value": ([d, d, i], d),
+            "fb_half_kernel_size": ([d, d, i], i),
+            "fb_sigma_effective": ([d, d, i], d),
+            "fb_workspace_size": ([i, i, i, i64, P, P, P, i, ctypes.POINTER(sz)], i),
+            "fb_interpolate": ([i, i, i, P, P, i64, P, P, P, P, i, d, P, i, P, sz, P], i),
+            "fb_interpolate_host": ([i, i, i, P, P, i64, P, P, P, P, i, d, P, i, P], i),
+            "fb_host_alloc": ([sz], P),
+            "fb_host_free": ([P], None),
+            "fb_release": ([], None),
+            "fb_accumulate_lines": ([i, P, i64, i64, i, i, d, i, P], i),
+            "fb_s2_workspace_size": ([i, i64, P, P, P, i, ctypes.POINTER(sz)], i),
+            "fb_interpolate_s2": ([i, P, P, i64, P, P, P, P, i, d, i, P, P, sz, P], i),
+            "fb_lambert_create_proj": ([d, d, d, d, P], None),
+            "fb_lambert_to_map": ([P, P, i64, P, P], i),
+            "fb_resample": ([P, i64, i64, P, P, P, P, P, P, P, P], i),
+            "fb_profile_begin": ([], i),
+            "fb_profile_end": ([P, P, i, ctypes.POINTER(i)], i),
+        }
+        for name, (args, res) in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+        return L
+
+
+def check(rc, what="fastbarnes_gb300"):
+    if rc != FB_OK:
+        msg = lib().fb_last_error().decode(errors="replace")
+        raise FastBarnesError(f"{what} failed (status {rc}): {msg}")
+
+
+def version():
+    return lib().fb_version().decode()
+
+
+# ---------------------------------------------------------------------------
+# device plumbing (torch provides device memory and the current stream)
+# ---------------------------------------------------------------------------
+
+_ws_cache = {}
+
+
+def torch_cuda():
+    import torch
+    if not torch.cuda.is_available():
+        raise FastBarnesError("no CUDA device available (fastbarnes_gb300 has no CPU fallback)")
+    return torch
+
+
+def workspace(nbytes, device):
+    """A cached uint8 device buffer of at least nbytes on `device`."""
+    torch = torch_cuda()
+    key = (device.index if device.index is not None else torch.cuda.current_device())
+    buf = _ws_cache.get(key)
+    if buf is None or buf.numel() < nbytes:
+        buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+        _ws_cache[key] = buf
+    return buf
+
+
+def stream_ptr(torch, device):
+    return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def dvec(values, ctype=ctypes.c_double):
+    arr = (ctype * len(values))(*values)
+    return arr

@@ -1,0 +1,151 @@
+/*
+ * fastbarnes_gb300.h -- C ABI of the GB300 fast Barnes interpolation library
+ * (libfastbarnes_gb300.so).
+ *
+ * Every entry point takes plain pointers and sizes.  Arrays named d_* are
+ * device pointers (CUDA global memory of the current device); everything else
+ * is host memory.  `stream` is a cudaStream_t passed as void* (NULL = the
+ * legacy default stream).  Device entry points are asynchronous on `stream`
+ * and never allocate: the caller provides the workspace whose size
+ * fb_workspace_size() reports.  Return value: FB_OK or one of the FB_ERR_*
+ * codes; fb_last_error() then holds a message for the calling thread.
+ *
+ * Layout conventions are the reference's (MeteoSwiss/fast-barnes-py 2.0):
+ *   pts  : N x dim float64, row-major (x, y[, z] of each sample)
+ *   val  : N float64
+ *   size : {nx[, ny[, nz]]} (x first), grid arrays are [nz][ny][nx], x fastest
+ */
+#ifndef FASTBARNES_GB300_H
+#define FASTBARNES_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum fb_status {
+    FB_OK = 0,
+    FB_ERR_ARG = 1,          /* invalid argument (dimension, sizes, pointers)     */
+    FB_ERR_KERNEL_SIZE = 2,  /* 2T+1 >= grid size in some axis                    */
+    FB_ERR_WORKSPACE = 3,    /* workspace missing or smaller than required        */
+    FB_ERR_CUDA = 4,         /* a CUDA runtime call failed                        */
+    FB_ERR_UNSUPPORTED = 5,  /* a line cannot be tiled in shared memory           */
+    FB_ERR_DEVICE = 6        /* a kernel reported an error through its status word */
+};
+
+enum fb_precision {
+    FB_FP64 = 0,   /* float64 throughout: the drop-in form                          */
+    FB_FP32C = 1   /* float32 running sums re-anchored on exact chunk sums, scaled  */
+};
+
+enum fb_method {
+    FB_OPTIMIZED_CONVOLUTION = 0,  /* 'optimized_convolution' (rect kernel + tails) */
+    FB_CONVOLUTION = 1             /* 'convolution' (plain rect kernel)             */
+};
+
+/* Library version string. */
+const char *fb_version(void);
+
+/* Message describing the last failure of the calling thread ("" if none). */
+const char *fb_last_error(void);
+
+/* ---- kernel-size helpers (host only) --------------------------------------
+ * Replace fastbarnes/interpolation.py:543-569 (get_half_kernel_size_opt,
+ * get_tail_value) and :777-803 (get_half_kernel_size, get_sigma_effective). */
+int fb_half_kernel_size_opt(double sigma, double step, int num_iter);
+double fb_tail_value(double sigma, double step, int num_iter);
+int fb_half_kernel_size(double sigma, double step, int num_iter);
+double fb_sigma_effective(double sigma, double step, int num_iter);
+
+/* ---- interpolation on a regular grid ---------------------------------------
+ * Replaces fastbarnes/interpolation.py:328-367 (_interpolate_opt_convol, for
+ * FB_OPTIMIZED_CONVOLUTION) and :575-612 (_interpolate_convol, for
+ * FB_CONVOLUTION), i.e. the body of barnes(..., method=...) after its
+ * argument checks (:31-199).  sigma, x0, step hold dim values, size dim
+ * values; max_dist_weight = exp(-max_dist^2 / 2) as computed at :167.
+ * d_out receives size[dim-1] x ... x size[0] values, float32 (out_f64 = 0,
+ * the reference's return type) or float64 (out_f64 = 1, the quotient before
+ * the float32 cast).  Grid points with too little weight are NaN (:420-430).
+ * Returns FB_ERR_KERNEL_SIZE when 2T+1 >= size[m] (the check of :170-175). */
+int fb_workspace_size(int method, int precision, int dim, int64_t n_pts, const double *sigma,
+                      const double *step, const int64_t *size, int num_iter, size_t *bytes);
+
+int fb_interpolate(int method, int precision, int dim, const double *d_pts, const double *d_val,
+                   int64_t n_pts, const double *sigma, const double *x0, const double *step,
+                   const int64_t *size, int num_iter, double max_dist_weight, void *d_out, int out_f64,
+                   void *d_workspace, size_t workspace_bytes, void *stream);
+
+/* Same computation from host buffers: copies pts / val to the device, runs
+ * fb_interpolate on `stream` with a library-owned device buffer (grown on
+ * demand, released by fb_release), copies the result into host `out` and
+ * synchronizes the stream.  Pinned host memory (fb_host_alloc) makes the
+ * copies asynchronous DMA transfers. */
+int fb_interpolate_host(int method, int precision, int dim, const double *pts, const double *val,
+                        int64_t n_pts, const double *sigma, const double *x0, const double *step,
+                        const int64_t *size, int num_iter, double max_dist_weight, void *out, int out_f64,
+                        void *stream);
+
+/* Pinned host memory for fb_interpolate_host buffers. */
+void *fb_host_alloc(size_t bytes);
+void fb_host_free(void *p);
+/* Frees the device buffers fb_interpolate_host keeps between calls. */
+void fb_release(void);
+
+/* ---- stage timing ---------------------------------------------------------
+ * No reference counterpart (the reference times whole calls with
+ * time.perf_counter_ns, demo/timing1_table1_figure4.py:107-115).  Between
+ * fb_profile_begin and fb_profile_end every interpolation records CUDA events
+ * around its stages on its stream; fb_profile_end waits for them and returns
+ * one record per stage: stage 0 = sample sort, 1 + m = the launch along axis
+ * m, with its elapsed milliseconds. */
+int fb_profile_begin(void);
+int fb_profile_end(int *stages, float *ms, int max_records, int *n_records);
+
+/* ---- the 1D rect-kernel passes alone -----------------------------------------
+ * Replaces _accumulate_tail_array (interpolation.py:484-533; rect_len = 2T+1,
+ * tail weight alpha) and _accumulate_array (:729-772; alpha = 0): num_iter
+ * passes over each of n_lines contiguous lines of length len, in place.  With
+ * normalize = 0 the sums are unscaled like the reference's; with 1 every pass
+ * is divided by rect_len + 2 alpha. */
+int fb_accumulate_lines(int precision, void *d_lines, int64_t n_lines, int64_t len, int rect_len,
+                        int num_iter, double alpha, int normalize, void *stream);
+
+/* ---- the sphere ---------------------------------------------------------------
+ * Replaces fastbarnes/interpolationS2.py:143-254 (_interpolate_opt_convol_S2:
+ * projection to the fixed Lambert grid x0 = (-32, -2), size =
+ * (int(64/step[0]), int(44/step[1])), optimized convolution there, and with
+ * resample = 1 the bilinear resampling back to the lon/lat grid).  d_out:
+ * size[1] x size[0] float32 (resample = 1) or the Lambert field
+ * int(44/step[1]) x int(64/step[0]) float32 (resample = 0). */
+int fb_s2_workspace_size(int precision, int64_t n_pts, const double *sigma, const double *step,
+                         const int64_t *size, int num_iter, size_t *bytes);
+int fb_interpolate_s2(int precision, const double *d_pts, const double *d_val, int64_t n_pts,
+                      const double *sigma, const double *x0, const double *step, const int64_t *size,
+                      int num_iter, double max_dist_weight, int resample, float *d_out, void *d_workspace,
+                      size_t workspace_bytes, void *stream);
+
+/* Replaces fastbarnes/util/lambert_conformal.py:50-94 (create_proj):
+ * proj[5] = {center_lon, n, n_inv, F, rho0}. */
+void fb_lambert_create_proj(double center_lon, double center_lat, double lat1, double lat2, double *proj);
+
+/* Replaces fastbarnes/util/lambert_conformal.py:113-123 (to_map) on the
+ * device: d_geo (lon, lat) pairs -> d_map (x, y) pairs. */
+int fb_lambert_to_map(const double *d_geo, double *d_map, int64_t n_pts, const double *proj, void *stream);
+
+/* Replaces fastbarnes/interpolationS2.py:211-254 (_resample) on the device:
+ * bilinear read of the float32 Lambert field d_lam (lam_h x lam_w, origin
+ * lam_x0, spacing step) at the projection of every point of the lon/lat grid
+ * (x0, step, size) into d_out (size[1] x size[0] float32).  d_tab is device
+ * scratch of size[1] + 2 * size[0] doubles.  Points whose Lambert cell lies
+ * outside the field are NaN (the reference does not check). */
+int fb_resample(const float *d_lam, int64_t lam_w, int64_t lam_h, const double *lam_x0, const double *x0,
+                const double *step, const int64_t *size, const double *proj, float *d_out, double *d_tab,
+                void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FASTBARNES_GB300_H */
