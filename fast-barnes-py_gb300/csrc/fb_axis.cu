@@ -93,6 +93,57 @@ __device__ __forceinline__ void slide(const Real *__restrict__ s, int E, int k0,
     }
 }
 
+// Narrow kernels (T <= TD_MAX): every output is summed directly from the
+// K + 2T + 2 inputs the chunk needs, held in registers.  Sliding a window of
+// only a few cells over 16 steps would carry the rounding error of large
+// values that have already left the window.
+template <typename Real, int K, int TD, bool GUARD>
+__device__ __forceinline__ void direct_pass(const Real *__restrict__ s, int E, int k0, const PassCoef<Real> &c,
+                                            Real (&o)[K])
+{
+    constexpr int NX = K + 2 * TD + 2;
+    Real x[NX];
+#pragma unroll
+    for (int m = 0; m < NX; m++)
+        x[m] = rd<GUARD>(s, k0 - TD - 1 + m, E);
+#pragma unroll
+    for (int i = 0; i < K; i++) {
+        Real acc = x[i + 1];
+#pragma unroll
+        for (int d = 2; d <= 2 * TD + 1; d++)
+            acc += x[i + d];
+        o[i] = c.out(acc, x[i] + x[i + 2 * TD + 2]);
+    }
+}
+
+template <typename Real>
+struct DirectMax;
+template <>
+struct DirectMax<float> {
+    static constexpr int T = 8;
+};
+template <>
+struct DirectMax<double> {
+    static constexpr int T = 3;
+};
+
+template <typename Real, int K, int TD>
+__device__ __forceinline__ bool try_direct(int T, const Real *s, int E, int k0, bool guard, const PassCoef<Real> &c,
+                                           Real (&o)[K])
+{
+    if constexpr (TD > DirectMax<Real>::T) {
+        return false;
+    } else {
+        if (T != TD)
+            return try_direct<Real, K, TD + 1>(T, s, E, k0, guard, c, o);
+        if (guard)
+            direct_pass<Real, K, TD, true>(s, E, k0, c, o);
+        else
+            direct_pass<Real, K, TD, false>(s, E, k0, c, o);
+        return true;
+    }
+}
+
 // Sums of a chunk used to build the next pass's anchors: the whole chunk (S),
 // its first r2 cells (Pre) and its cells from r1 on (Suf).  Cells at or beyond
 // the line extent count as zero.
@@ -326,8 +377,9 @@ __global__ void __launch_bounds__(1024, 1) k_axis(const AxisLaunch a, const Geom
     Real *ln_ = sm + lf * P;                  // this thread's line buffer
     Real *pp = part + (size_t)lf * 3 * CP;    // S | Pre | Suf of that line
 
-    // partials of the filled data
-    if (active) {
+    const bool direct = T <= DirectMax<Real>::T;
+    // partials of the filled data (anchors of the first sliding pass)
+    if (active && !direct) {
         Real o[K];
 #pragma unroll
         for (int i = 0; i < K; i++)
@@ -345,18 +397,18 @@ __global__ void __launch_bounds__(1024, 1) k_axis(const AxisLaunch a, const Geom
         Real o[K];
         Real S = 0, Pr = 0, Su = 0;
         if (active) {
-            Real A0, A1;
-            if (T == 0) {
-                A0 = rd<true>(ln_, k0, E);
-                A1 = rd<true>(ln_, k0 + K, E);
+            const bool guard = (k0 - T - 1 < 0) || (k0 + K + T >= E);
+            if (direct) {
+                try_direct<Real, K, 0>(T, ln_, E, k0, guard, coef, o);
             } else {
+                Real A0, A1;
                 anchors(pp, pp + CP, pp + 2 * CP, nch, j, d1, d2, A0, A1);
+                if (guard)
+                    slide<Real, K, true>(ln_, E, k0, T, A0, A1, coef, o);
+                else
+                    slide<Real, K, false>(ln_, E, k0, T, A0, A1, coef, o);
+                chunk_partials<Real, K>(o, k0, E, r1, r2, S, Pr, Su);
             }
-            if ((k0 - T - 1 < 0) || (k0 + K + T >= E))
-                slide<Real, K, true>(ln_, E, k0, T, A0, A1, coef, o);
-            else
-                slide<Real, K, false>(ln_, E, k0, T, A0, A1, coef, o);
-            chunk_partials<Real, K>(o, k0, E, r1, r2, S, Pr, Su);
         }
         __syncthreads();
         if (active) {
@@ -370,9 +422,11 @@ __global__ void __launch_bounds__(1024, 1) k_axis(const AxisLaunch a, const Geom
                     if (k0 + i < E)
                         ln_[k0 + i] = o[i];
             }
-            pp[j] = S;
-            pp[CP + j] = Pr;
-            pp[2 * CP + j] = Su;
+            if (!direct) {
+                pp[j] = S;
+                pp[CP + j] = Pr;
+                pp[2 * CP + j] = Su;
+            }
         }
     }
     __syncthreads();
