@@ -29,17 +29,6 @@
 
 namespace fbg {
 
-template <typename Real>
-struct Chunk;
-template <>
-struct Chunk<float> {
-    static constexpr int K = K32;
-};
-template <>
-struct Chunk<double> {
-    static constexpr int K = K64;
-};
-
 template <bool GUARD, typename Real>
 __device__ __forceinline__ Real rd(const Real *__restrict__ s, int e, int E)
 {
@@ -305,11 +294,11 @@ __device__ void splat_line(Real *lv, Real *lw, int E, int64_t e0, int64_t line, 
 }
 
 // SPLAT_DIM: 0 = the lines are loaded from src_v / src_w, 1..3 = they are
-// filled by splatting the samples of a field of that dimension.
-template <typename Real, int SPLAT_DIM>
+// filled by splatting the samples of a field of that dimension.  K: chunk
+// length (odd), chosen per launch by chunk_k().
+template <typename Real, int K, int SPLAT_DIM>
 __global__ void __launch_bounds__(1024, 1) k_axis(const AxisLaunch a, const Geometry g, const SampleView sv)
 {
-    constexpr int K = Chunk<Real>::K;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Real *sm = reinterpret_cast<Real *>(smem_raw);
     const int NL = a.lines_per_cta;
@@ -377,7 +366,8 @@ __global__ void __launch_bounds__(1024, 1) k_axis(const AxisLaunch a, const Geom
     Real *ln_ = sm + lf * P;                  // this thread's line buffer
     Real *pp = part + (size_t)lf * 3 * CP;    // S | Pre | Suf of that line
 
-    const bool direct = T <= DirectMax<Real>::T;
+    // direct sums only in the short-chunk kernels (the long chunk serves T > 32)
+    const bool direct = (K == K64) && T <= DirectMax<Real>::T;
     // partials of the filled data (anchors of the first sliding pass)
     if (active && !direct) {
         Real o[K];
@@ -398,9 +388,11 @@ __global__ void __launch_bounds__(1024, 1) k_axis(const AxisLaunch a, const Geom
         Real S = 0, Pr = 0, Su = 0;
         if (active) {
             const bool guard = (k0 - T - 1 < 0) || (k0 + K + T >= E);
-            if (direct) {
-                try_direct<Real, K, 0>(T, ln_, E, k0, guard, coef, o);
-            } else {
+            if constexpr (K == K64) {
+                if (direct)
+                    try_direct<Real, K, 0>(T, ln_, E, k0, guard, coef, o);
+            }
+            if (!direct) {
                 Real A0, A1;
                 anchors(pp, pp + CP, pp + 2 * CP, nch, j, d1, d2, A0, A1);
                 if (guard)
@@ -485,7 +477,16 @@ __global__ void __launch_bounds__(1024, 1) k_axis(const AxisLaunch a, const Geom
 // host side
 // ---------------------------------------------------------------------------
 
-static int chunk_k(int precision) { return precision == 0 ? K64 : K32; }
+// Chunk length per launch.  Every output is at most K/2 sliding steps from an
+// exact anchor; in float32 that distance must stay short against the window
+// 2T+1, so windows up to 65 cells use the short chunk (and T <= 8 sums
+// directly), wider ones the long chunk with half the anchor overhead.
+static int chunk_k(int precision, int T)
+{
+    if (precision == 0)
+        return K64;
+    return T <= 32 ? K64 : K32;
+}
 static int real_size(int precision) { return precision == 0 ? 8 : 4; }
 
 static size_t smem_limit()
@@ -501,11 +502,11 @@ static size_t smem_limit()
     return (size_t)lim;
 }
 
-AxisPlanLimits axis_limits(int precision)
+AxisPlanLimits axis_limits(int precision, int T)
 {
     AxisPlanLimits l;
     l.smem_limit = smem_limit();
-    const int K = chunk_k(precision), sz = real_size(precision);
+    const int K = chunk_k(precision, T), sz = real_size(precision);
     // largest extent E with one line per CTA: threads and shared memory
     // a line takes two thread groups (value, weight) of chunks_pad threads
     int e_thr = kMaxLineThreads / 2 * K;
@@ -533,7 +534,7 @@ size_t axis_smem_bytes(int precision, const AxisLaunch &a)
 
 bool axis_shape(int precision, AxisLaunch &a)
 {
-    const int K = chunk_k(precision);
+    const int K = chunk_k(precision, a.T);
     int64_t E = a.tile_len + 2 * (int64_t)a.halo;
     if (E > a.L)
         E = a.L;
@@ -560,13 +561,13 @@ bool axis_shape(int precision, AxisLaunch &a)
     return axis_smem_bytes(precision, a) <= smem_limit();
 }
 
-template <typename Real, int SD>
+template <typename Real, int K, int SD>
 static cudaError_t launch_one(const AxisLaunch &a, const Geometry &g, const SampleView &sv, cudaStream_t st)
 {
     const size_t smem = axis_smem_bytes(sizeof(Real) == 8 ? 0 : 1, a);
     static size_t configured = 0;
     if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_axis<Real, SD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(k_axis<Real, K, SD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem_limit());
         if (e != cudaSuccess)
             return e;
@@ -575,28 +576,30 @@ static cudaError_t launch_one(const AxisLaunch &a, const Geometry &g, const Samp
     const int64_t groups = (a.nlines + a.lines_per_cta - 1) / a.lines_per_cta;
     const int64_t blocks = groups * a.ntiles;
     const int threads = a.lines_per_cta * 2 * a.chunks_pad;
-    k_axis<Real, SD><<<(unsigned)blocks, threads, smem, st>>>(a, g, sv);
+    k_axis<Real, K, SD><<<(unsigned)blocks, threads, smem, st>>>(a, g, sv);
     return cudaGetLastError();
+}
+
+template <typename Real, int K>
+static cudaError_t launch_k(int sd, const AxisLaunch &a, const Geometry &g, const SampleView &sv, cudaStream_t st)
+{
+    switch (sd) {
+    case 0: return launch_one<Real, K, 0>(a, g, sv, st);
+    case 1: return launch_one<Real, K, 1>(a, g, sv, st);
+    case 2: return launch_one<Real, K, 2>(a, g, sv, st);
+    default: return launch_one<Real, K, 3>(a, g, sv, st);
+    }
 }
 
 cudaError_t launch_axis(int precision, const AxisLaunch &a, const Geometry &g, const SampleView &sv,
                         cudaStream_t st)
 {
     const int sd = a.fill_splat ? g.dim : 0;
-    if (precision == 0) {
-        switch (sd) {
-        case 0: return launch_one<double, 0>(a, g, sv, st);
-        case 1: return launch_one<double, 1>(a, g, sv, st);
-        case 2: return launch_one<double, 2>(a, g, sv, st);
-        default: return launch_one<double, 3>(a, g, sv, st);
-        }
-    }
-    switch (sd) {
-    case 0: return launch_one<float, 0>(a, g, sv, st);
-    case 1: return launch_one<float, 1>(a, g, sv, st);
-    case 2: return launch_one<float, 2>(a, g, sv, st);
-    default: return launch_one<float, 3>(a, g, sv, st);
-    }
+    if (precision == 0)
+        return launch_k<double, K64>(sd, a, g, sv, st);
+    if (chunk_k(precision, a.T) == K64)
+        return launch_k<float, K64>(sd, a, g, sv, st);
+    return launch_k<float, K32>(sd, a, g, sv, st);
 }
 
 cudaError_t launch_lines(int precision, void *data, int64_t nlines, int64_t len, int T, double alpha, int passes,

@@ -174,11 +174,11 @@ int make_plan(int method, int precision, int dim, int64_t npts, const double *si
     }
 
     // per-axis launches; `cur` tracks which buffer pair holds the data
-    const AxisPlanLimits lim = axis_limits(precision);
     int cur = -1;   // -1: nothing yet (first launch splats)
     for (int m = 0; m < dim; m++) {
         const int64_t L = size[m];
         const int T = g.T[m];
+        const AxisPlanLimits lim = axis_limits(precision, T);
         std::vector<AxisLaunch> axl;
         AxisLaunch a{};
         a.axis = m;
@@ -547,7 +547,7 @@ extern "C" int fb_accumulate_lines(int precision, void *d_lines, int64_t n_lines
         return fail(FB_ERR_ARG, "invalid line arguments");
     if (n_lines == 0 || num_iter == 0)
         return FB_OK;
-    const AxisPlanLimits lim = axis_limits(precision);
+    const AxisPlanLimits lim = axis_limits(precision, (rect_len - 1) / 2);
     if (len > lim.extent_max)
         return fail(FB_ERR_UNSUPPORTED, "line length %lld exceeds %d", (long long)len, lim.extent_max);
     cudaError_t e = launch_lines(precision, d_lines, n_lines, len, (rect_len - 1) / 2, alpha, num_iter, normalize,

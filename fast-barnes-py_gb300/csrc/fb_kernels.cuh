@@ -15,7 +15,8 @@ struct AxisPlanLimits {
     int extent_max;      // longest line extent held in shared memory
     size_t smem_limit;   // dynamic shared memory per block
 };
-AxisPlanLimits axis_limits(int precision);
+// Longest line extent one CTA holds for half kernel width T.
+AxisPlanLimits axis_limits(int precision, int T);
 // Shared memory needed by one CTA of a launch.
 size_t axis_smem_bytes(int precision, const AxisLaunch &a);
 // Fills in lines_per_cta, extent_max, line_pitch, chunks_pad for a launch
