@@ -188,6 +188,8 @@ def main():
     ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quick", action="store_true",
+                    help="warm-up and timed steps only (no fp64 form, e2e or CPU baseline): for profiler runs")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
@@ -277,6 +279,12 @@ def main():
     achieved = alg[dom] / (stage_ms[dom] / 1e3) / 1e9
     pipeline_bytes = NPTS * 28 + W * H * (4 * sz + 4)
     pipeline_gbs = pipeline_bytes * B * args.steps / (t_ms / 1e3) / 1e9
+
+    if args.quick:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": "Mgridpts/s", "quick": True,
+                              "stage_ms": {names[k]: v for k, v in stage_ms.items()}}), flush=True)
+        return
 
     # ---- plain float64 form of the same batch + error at fixed config -----
     ws64 = ws_for(_lib.FB_FP64) if prec != _lib.FB_FP64 else ws
