@@ -29,72 +29,76 @@
 
 namespace fbg {
 
-template <bool GUARD, typename Real>
+// ---------------------------------------------------------------------------
+// one line of one field, seen by one thread: cell e lives at s[e * ES]
+// ---------------------------------------------------------------------------
+
+template <bool GUARD, int ES, typename Real>
 __device__ __forceinline__ Real rd(const Real *__restrict__ s, int e, int E)
 {
     if (GUARD)
-        return (unsigned)e < (unsigned)E ? s[e] : Real(0);
-    return s[e];
+        return (unsigned)e < (unsigned)E ? s[e * ES] : Real(0);
+    return s[e * ES];
 }
 
-template <typename Real>
+template <typename Real, bool SCALED>
 struct PassCoef {
-    Real alpha;   // tail weight (unscaled form) or alpha / (2T+1+2alpha) (scaled form)
-    Real inv;     // 1 (unscaled) or 1 / (2T+1+2alpha)
-    bool scaled;
+    Real alpha;   // tail weight (alpha * inv when scaled)
+    Real inv;     // 1 / (2T+1+2alpha)
     __device__ __forceinline__ Real out(Real acc, Real tails) const
     {
-        return scaled ? fma(acc, inv, alpha * tails) : fma(alpha, tails, acc);
+        if (SCALED)
+            return fma(acc, inv, alpha * tails);
+        return fma(alpha, tails, acc);
     }
 };
 
-// Slides the window over the chunk [k0, k0 + K) of one line: forward from A0
-// (window at k0) over the first half, backward from A1 (window at k0 + K) over
-// the second half.
-template <typename Real, int K, bool GUARD>
+// Slides the window over the chunk [k0, k0 + K): forward from A0 (window at
+// k0) over the first half, backward from A1 (window at k0 + K) over the rest.
+template <typename Real, int K, int ES, bool GUARD, bool SCALED>
 __device__ __forceinline__ void slide(const Real *__restrict__ s, int E, int k0, int T, Real A0, Real A1,
-                                      const PassCoef<Real> &c, Real (&o)[K])
+                                      const PassCoef<Real, SCALED> &c, Real (&o)[K])
 {
     constexpr int H = K / 2;
     Real acc = A0;
-    Real prev = rd<GUARD>(s, k0 - T - 1, E);
+    Real prev = rd<GUARD, ES>(s, k0 - T - 1, E);
 #pragma unroll
     for (int i = 0; i < H; i++) {
         const int k = k0 + i;
-        const Real nw = rd<GUARD>(s, k + T + 1, E);
-        const Real od = rd<GUARD>(s, k - T, E);
+        const Real nw = rd<GUARD, ES>(s, k + T + 1, E);
+        const Real od = rd<GUARD, ES>(s, k - T, E);
         o[i] = c.out(acc, prev + nw);
         acc += nw;
         acc -= od;
         prev = od;
     }
     acc = A1;
-    Real od = rd<GUARD>(s, k0 + K - 1 - T, E);
+    Real od = rd<GUARD, ES>(s, k0 + K - 1 - T, E);
 #pragma unroll
     for (int i = K - 1; i >= H; i--) {
         const int k = k0 + i;
-        const Real nw = rd<GUARD>(s, k + T + 1, E);
+        const Real nw = rd<GUARD, ES>(s, k + T + 1, E);
         acc -= nw;
         acc += od;
-        const Real tl = rd<GUARD>(s, k - T - 1, E);
+        const Real tl = rd<GUARD, ES>(s, k - T - 1, E);
         o[i] = c.out(acc, tl + nw);
         od = tl;
     }
 }
 
-// Narrow kernels (T <= TD_MAX): every output is summed directly from the
+// Narrow kernels (T <= DirectMax): every output is summed directly from the
 // K + 2T + 2 inputs the chunk needs, held in registers.  Sliding a window of
-// only a few cells over 16 steps would carry the rounding error of large
+// only a few cells over K/2 steps would carry the rounding error of large
 // values that have already left the window.
-template <typename Real, int K, int TD, bool GUARD>
-__device__ __forceinline__ void direct_pass(const Real *__restrict__ s, int E, int k0, const PassCoef<Real> &c,
-                                            Real (&o)[K])
+template <typename Real, int K, int ES, int TD, bool GUARD, bool SCALED>
+__device__ __forceinline__ void direct_pass(const Real *__restrict__ s, int E, int k0,
+                                            const PassCoef<Real, SCALED> &c, Real (&o)[K])
 {
     constexpr int NX = K + 2 * TD + 2;
     Real x[NX];
 #pragma unroll
     for (int m = 0; m < NX; m++)
-        x[m] = rd<GUARD>(s, k0 - TD - 1 + m, E);
+        x[m] = rd<GUARD, ES>(s, k0 - TD - 1 + m, E);
 #pragma unroll
     for (int i = 0; i < K; i++) {
         Real acc = x[i + 1];
@@ -116,53 +120,55 @@ struct DirectMax<double> {
     static constexpr int T = 3;
 };
 
-template <typename Real, int K, int TD>
-__device__ __forceinline__ bool try_direct(int T, const Real *s, int E, int k0, bool guard, const PassCoef<Real> &c,
-                                           Real (&o)[K])
+template <typename Real, int K, int ES, int TD, bool SCALED>
+__device__ __forceinline__ void direct_dispatch(int T, const Real *s, int E, int k0, bool guard,
+                                                const PassCoef<Real, SCALED> &c, Real (&o)[K])
 {
-    if constexpr (TD > DirectMax<Real>::T) {
-        return false;
-    } else {
-        if (T != TD)
-            return try_direct<Real, K, TD + 1>(T, s, E, k0, guard, c, o);
+    if constexpr (TD <= DirectMax<Real>::T) {
+        if (T != TD) {
+            direct_dispatch<Real, K, ES, TD + 1, SCALED>(T, s, E, k0, guard, c, o);
+            return;
+        }
         if (guard)
-            direct_pass<Real, K, TD, true>(s, E, k0, c, o);
+            direct_pass<Real, K, ES, TD, true, SCALED>(s, E, k0, c, o);
         else
-            direct_pass<Real, K, TD, false>(s, E, k0, c, o);
-        return true;
+            direct_pass<Real, K, ES, TD, false, SCALED>(s, E, k0, c, o);
     }
 }
 
-// Sums of a chunk used to build the next pass's anchors: the whole chunk (S),
-// its first r2 cells (Pre) and its cells from r1 on (Suf).  Cells at or beyond
-// the line extent count as zero.
-template <typename Real, int K>
+// Sums of a chunk that the next pass's anchors are built from: the whole
+// chunk (S), its first r2 cells (Pre) and its cells from r1 on (Suf).  Cells
+// at or beyond the line extent count as zero (tail chunk only).
+template <typename Real, int K, bool TAIL>
 __device__ __forceinline__ void chunk_partials(const Real (&o)[K], int k0, int E, int r1, int r2, Real &S,
                                                Real &Pre, Real &Suf)
 {
     Real s = 0, p = 0, u = 0;
 #pragma unroll
     for (int i = 0; i < K; i++) {
-        const Real x = (k0 + i < E) ? o[i] : Real(0);
+        const Real x = (!TAIL || k0 + i < E) ? o[i] : Real(0);
         s += x;
-        p += (i < r2) ? x : Real(0);
-        u += (i >= r1) ? x : Real(0);
+        if (i < r2)
+            p += x;
+        if (i >= r1)
+            u += x;
     }
     S = s;
     Pre = p;
     Suf = u;
 }
 
-template <typename Real>
+template <typename Real, int PS>
 __device__ __forceinline__ Real part_at(const Real *__restrict__ a, int m, int nch)
 {
-    return (unsigned)m < (unsigned)nch ? a[m] : Real(0);
+    return (unsigned)m < (unsigned)nch ? a[m * PS] : Real(0);
 }
 
 // Window sums at k0 = jK and k0 + K from the chunk partials (T >= 1):
 // window [k0-T, k0+T] = Suf[m1] + S[m1+1 .. m2-1] + Pre[m2], m1 = j - d1,
-// m2 = j + d2 (d1 = ceil(T/K), d2 = floor((T+1)/K)).
-template <typename Real>
+// m2 = j + d2 (d1 = ceil(T/K), d2 = floor((T+1)/K)).  Every term is a sum of
+// cells inside the window: nothing is subtracted.
+template <typename Real, int PS>
 __device__ __forceinline__ void anchors(const Real *__restrict__ S, const Real *__restrict__ Pre,
                                         const Real *__restrict__ Suf, int nch, int j, int d1, int d2,
                                         Real &A0, Real &A1)
@@ -170,21 +176,52 @@ __device__ __forceinline__ void anchors(const Real *__restrict__ S, const Real *
     const int m1 = j - d1, m2 = j + d2;
     Real mid = 0;
     for (int m = m1 + 2; m <= m2 - 1; m++)
-        mid += part_at(S, m, nch);
+        mid += part_at<Real, PS>(S, m, nch);
     const bool two = (m2 - m1) >= 2;
-    A0 = part_at(Suf, m1, nch) + (two ? part_at(S, m1 + 1, nch) : Real(0)) + mid + part_at(Pre, m2, nch);
-    A1 = part_at(Suf, m1 + 1, nch) + mid + (two ? part_at(S, m2, nch) : Real(0)) + part_at(Pre, m2 + 1, nch);
+    A0 = part_at<Real, PS>(Suf, m1, nch) + (two ? part_at<Real, PS>(S, m1 + 1, nch) : Real(0)) + mid +
+         part_at<Real, PS>(Pre, m2, nch);
+    A1 = part_at<Real, PS>(Suf, m1 + 1, nch) + mid + (two ? part_at<Real, PS>(S, m2, nch) : Real(0)) +
+         part_at<Real, PS>(Pre, m2 + 1, nch);
 }
 
-__device__ __forceinline__ int64_t line_base(const AxisLaunch &a, const Geometry &g, int64_t line)
+// One box pass of one thread's chunk: outputs into o, next partials into S/P/U.
+template <typename Real, int K, int ES, int PS, bool SCALED>
+__device__ __forceinline__ void run_pass(const Real *__restrict__ ln, const Real *__restrict__ pp, int QS, int E,
+                                         int nch, int j, int T, int d1, int d2, int r1, int r2, bool direct,
+                                         const PassCoef<Real, SCALED> &c, Real (&o)[K], Real &S, Real &P, Real &U)
 {
-    if (a.axis == 0)
-        return line * a.L;
-    if (a.axis == 1) {
-        const int64_t W = g.size[0];
-        return (line / W) * (W * g.size[1]) + (line % W);
+    const int k0 = j * K;
+    const bool guard = (k0 - T - 1 < 0) || (k0 + K + T >= E);
+    if constexpr (K == K64) {
+        if (direct) {
+            direct_dispatch<Real, K, ES, 0, SCALED>(T, ln, E, k0, guard, c, o);
+            return;
+        }
     }
-    return line;
+    Real A0, A1;
+    anchors<Real, PS>(pp, pp + QS, pp + 2 * QS, nch, j, d1, d2, A0, A1);
+    if (guard)
+        slide<Real, K, ES, true, SCALED>(ln, E, k0, T, A0, A1, c, o);
+    else
+        slide<Real, K, ES, false, SCALED>(ln, E, k0, T, A0, A1, c, o);
+    if (k0 + K <= E)
+        chunk_partials<Real, K, false>(o, k0, E, r1, r2, S, P, U);
+    else
+        chunk_partials<Real, K, true>(o, k0, E, r1, r2, S, P, U);
+}
+
+template <typename Real>
+__device__ __forceinline__ Real quotient(Real v, Real w, Real thr, double offset);
+template <>
+__device__ __forceinline__ double quotient<double>(double v, double w, double thr, double offset)
+{
+    // NaN where the weight is below the mask level, else vg / wg + offset
+    return (w < thr) ? __longlong_as_double(0x7ff8000000000000ll) : v / w + offset;
+}
+template <>
+__device__ __forceinline__ float quotient<float>(float v, float w, float thr, double offset)
+{
+    return (w < thr) ? __int_as_float(0x7fc00000) : v / w + (float)offset;
 }
 
 // Accumulates the contributions of the samples in sorted positions [beg, end)
@@ -293,23 +330,46 @@ __device__ void splat_line(Real *lv, Real *lw, int E, int64_t e0, int64_t line, 
     }
 }
 
+// ---------------------------------------------------------------------------
+// the kernel
+// ---------------------------------------------------------------------------
+
+template <int G, typename Real>
+struct Vec;   // 16-byte vector of Real
+template <int G>
+struct Vec<G, float> {
+    using T = float4;
+};
+template <int G>
+struct Vec<G, double> {
+    using T = double2;
+};
+
+// Column-layout group width: 32 bytes of each line-segment row.
+template <typename Real>
+struct ColG {
+    static constexpr int G = 32 / sizeof(Real);
+};
+
 // SPLAT_DIM: 0 = the lines are loaded from src_v / src_w, 1..3 = they are
-// filled by splatting the samples of a field of that dimension.  K: chunk
-// length (odd), chosen per launch by chunk_k().
-template <typename Real, int K, int SPLAT_DIM>
+// filled by splatting the samples of a field of that dimension (rows layout).
+// LAYOUT: 0 = rows, 1 = columns.  K: chunk length (odd).
+template <typename Real, int K, int SPLAT_DIM, int LAYOUT>
 __global__ void __launch_bounds__(1024, 1) k_axis(const AxisLaunch a, const Geometry g, const SampleView sv)
 {
+    constexpr int G = ColG<Real>::G;
+    constexpr int ES = LAYOUT == 0 ? 1 : G;   // cell stride inside a line buffer
+    constexpr int PS = LAYOUT == 0 ? 1 : G;   // chunk stride inside a partials array
+    constexpr int VPR = 16 / sizeof(Real);    // cells per 16-byte vector
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Real *sm = reinterpret_cast<Real *>(smem_raw);
-    const int NL = a.lines_per_cta;
     const int P = a.line_pitch;
     const int CP = a.chunks_pad;
-    Real *part = sm + (size_t)NL * 2 * P;   // [NL][2][3][CP]
+    const int tid = threadIdx.x;
+    const int nthr = blockDim.x;
 
     const int64_t group = blockIdx.x / a.ntiles;
-    const int64_t tile = blockIdx.x % a.ntiles;
-    const int64_t line0 = group * NL;
-    const int nl = (int)min((int64_t)NL, a.nlines - line0);
+    const int64_t tile = blockIdx.x - group * a.ntiles;
     const int64_t t0 = tile * a.tile_len;
     const int64_t t1 = min(a.L, t0 + a.tile_len);
     const int64_t e0 = max((int64_t)0, t0 - (int64_t)a.halo);
@@ -317,107 +377,153 @@ __global__ void __launch_bounds__(1024, 1) k_axis(const AxisLaunch a, const Geom
     const int E = (int)(e1 - e0);
     const int nch = (E + K - 1) / K;
 
-    const int tid = threadIdx.x;
-    const int lf = tid / CP;   // (line, field) of this thread: line lf / 2, field lf % 2
-    const int my = lf >> 1;
-    const int j = tid - lf * CP;
-    const bool active = my < nl && j < nch;
-    const int k0 = j * K;
+    // lines of this CTA and their HBM base (cell e0 of the line)
+    int nl;                  // lines present
+    int64_t line0 = 0;       // rows: first line index
+    int64_t gbase = 0;       // columns: HBM index of (line 0 of the group, cell e0)
+    bool vec_ok = false;     // columns: 16-byte row segments are aligned
+    if (LAYOUT == 0) {
+        line0 = group * a.lines_per_cta;
+        nl = (int)min((int64_t)a.lines_per_cta, a.nlines - line0);
+    } else {
+        const int64_t o = group / a.xblocks, xb = group - o * a.xblocks;
+        nl = (int)min((int64_t)G, a.width - xb * G);
+        gbase = o * a.outer_stride + xb * G + e0 * a.elem_stride;
+        vec_ok = nl == G && (gbase % VPR) == 0 && (a.elem_stride % VPR) == 0;
+    }
+
+    // this thread's line / field / chunk
+    int lf, f, ln_i, j;
+    Real *ln;
+    Real *pp;
+    int QS;
+    if (LAYOUT == 0) {
+        lf = tid / CP;
+        j = tid - lf * CP;
+        f = lf & 1;
+        ln_i = lf >> 1;
+        ln = sm + (size_t)lf * P;
+        QS = CP;
+        pp = sm + (size_t)a.lines_per_cta * 2 * P + (size_t)lf * 3 * CP + j;
+    } else {
+        const int tpf = G * CP;
+        f = tid / tpf;
+        const int r = tid - f * tpf;
+        ln_i = r % G;
+        j = r / G;
+        lf = f;
+        ln = sm + (size_t)f * P * G + ln_i;
+        QS = CP * G;
+        pp = sm + (size_t)2 * P * G + (size_t)f * 3 * CP * G + ln_i + (size_t)j * G;
+    }
+    // pp points at S[j]; the anchors index relative to chunk 0
+    Real *pp0 = pp - (size_t)j * PS;
+    const bool active = ln_i < nl && j < nch && f < 2;
     const int T = a.T;
     const int d1 = (T + K - 1) / K, d2 = (T + 1) / K;
     const int r1 = d1 * K - T, r2 = (T + 1) - d2 * K;
     const double offset = (SPLAT_DIM != 0 || a.store_quot) ? field_offset(sv.hdr) : 0.0;
 
     // ---- fill -------------------------------------------------------------
-    if (SPLAT_DIM == 0) {
-        const Real *sv_ = reinterpret_cast<const Real *>(a.src_v);
-        const Real *sw_ = reinterpret_cast<const Real *>(a.src_w);
-        if (a.axis == 0) {
-            for (int ln = 0; ln < nl; ln++) {
-                const int64_t b = line_base(a, g, line0 + ln) + e0;
-                for (int e = tid; e < E; e += blockDim.x) {
-                    sm[(ln * 2 + 0) * P + e] = sv_[b + e];
-                    sm[(ln * 2 + 1) * P + e] = sw_[b + e];
+    if (SPLAT_DIM != 0) {
+        // rows layout: zero the line buffers, then one warp per line splats
+        float4 *z4 = reinterpret_cast<float4 *>(sm);
+        const int n4 = (int)((size_t)a.lines_per_cta * 2 * P * sizeof(Real) / 16);
+        for (int i = tid; i < n4; i += nthr)
+            z4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        __syncthreads();
+        if (ln_i < nl && f == 0 && j < 32)
+            splat_line<Real, SPLAT_DIM>(sm + (size_t)(ln_i * 2) * P, sm + (size_t)(ln_i * 2 + 1) * P, E, e0,
+                                        line0 + ln_i, g, sv, offset, j);
+    } else if (LAYOUT == 0) {
+        const Real *src[2] = {reinterpret_cast<const Real *>(a.src_v), reinterpret_cast<const Real *>(a.src_w)};
+        for (int q = 0; q < 2 * nl; q++) {
+            const Real *s_ = src[q & 1] + (line0 + (q >> 1)) * a.L + e0;
+            Real *d_ = sm + (size_t)((q >> 1) * 2 + (q & 1)) * P;
+            for (int e = tid; e < E; e += nthr)
+                d_[e] = s_[e];
+        }
+    } else {
+        const Real *src[2] = {reinterpret_cast<const Real *>(a.src_v), reinterpret_cast<const Real *>(a.src_w)};
+        const int64_t es = a.elem_stride;
+        if (vec_ok) {
+            using V = typename Vec<G, Real>::T;
+            constexpr int VR = G / VPR;   // vectors per row (2)
+            const int nv = E * VR;
+#pragma unroll 1
+            for (int ff = 0; ff < 2; ff++) {
+                V *d_ = reinterpret_cast<V *>(sm + (size_t)ff * P * G);
+                const Real *s_ = src[ff] + gbase;
+#pragma unroll 4
+                for (int i = tid; i < nv; i += nthr) {
+                    const int row = i / VR, h = i - row * VR;
+                    d_[i] = *reinterpret_cast<const V *>(s_ + row * es + h * VPR);
                 }
             }
         } else {
-            const int64_t st = a.elem_stride;
-            for (int idx = tid; idx < nl * E; idx += blockDim.x) {
-                const int ln = idx % nl, e = idx / nl;
-                const int64_t gi = line_base(a, g, line0 + ln) + (e0 + e) * st;
-                sm[(ln * 2 + 0) * P + e] = sv_[gi];
-                sm[(ln * 2 + 1) * P + e] = sw_[gi];
+            for (int ff = 0; ff < 2; ff++) {
+                Real *d_ = sm + (size_t)ff * P * G;
+                const Real *s_ = src[ff] + gbase;
+                for (int i = tid; i < E * G; i += nthr) {
+                    const int row = i / G, gg = i - row * G;
+                    d_[i] = gg < nl ? s_[row * es + gg] : Real(0);
+                }
             }
         }
-    } else {
-        for (int ln = 0; ln < nl; ln++)
-            for (int e = tid; e < E; e += blockDim.x) {
-                sm[(ln * 2 + 0) * P + e] = Real(0);
-                sm[(ln * 2 + 1) * P + e] = Real(0);
-            }
-        __syncthreads();
-        // the first warp of every line's value-field threads splats that line
-        if (my < nl && (lf & 1) == 0 && j < 32)
-            splat_line<Real, SPLAT_DIM>(sm + (my * 2 + 0) * P, sm + (my * 2 + 1) * P, E, e0, line0 + my, g, sv,
-                                        offset, j);
     }
     __syncthreads();
 
-    Real *ln_ = sm + lf * P;                  // this thread's line buffer
-    Real *pp = part + (size_t)lf * 3 * CP;    // S | Pre | Suf of that line
-
-    // direct sums only in the short-chunk kernels (the long chunk serves T > 32)
+    // ---- passes -----------------------------------------------------------
     const bool direct = (K == K64) && T <= DirectMax<Real>::T;
-    // partials of the filled data (anchors of the first sliding pass)
     if (active && !direct) {
+        // partials of the filled data
         Real o[K];
+        const int k0 = j * K;
 #pragma unroll
         for (int i = 0; i < K; i++)
-            o[i] = (k0 + i < E) ? ln_[min(k0 + i, E - 1)] : Real(0);
-        chunk_partials<Real, K>(o, k0, E, r1, r2, pp[j], pp[CP + j], pp[2 * CP + j]);
+            o[i] = (k0 + i < E) ? ln[(k0 + i) * ES] : Real(0);
+        Real S, Pr, Su;
+        chunk_partials<Real, K, true>(o, k0, E, r1, r2, S, Pr, Su);
+        pp[0] = S;
+        pp[QS] = Pr;
+        pp[2 * QS] = Su;
     }
 
-    PassCoef<Real> coef;
-    coef.scaled = a.inv_norm != 1.0;
-    coef.inv = (Real)a.inv_norm;
-    coef.alpha = coef.scaled ? (Real)(a.alpha * a.inv_norm) : (Real)a.alpha;
+    PassCoef<Real, false> cu;
+    cu.alpha = (Real)a.alpha;
+    cu.inv = (Real)1;
+    PassCoef<Real, true> cs;
+    cs.alpha = (Real)(a.alpha * a.inv_norm);
+    cs.inv = (Real)a.inv_norm;
 
     for (int pass = 0; pass < a.passes; pass++) {
         __syncthreads();
         Real o[K];
         Real S = 0, Pr = 0, Su = 0;
         if (active) {
-            const bool guard = (k0 - T - 1 < 0) || (k0 + K + T >= E);
-            if constexpr (K == K64) {
-                if (direct)
-                    try_direct<Real, K, 0>(T, ln_, E, k0, guard, coef, o);
-            }
-            if (!direct) {
-                Real A0, A1;
-                anchors(pp, pp + CP, pp + 2 * CP, nch, j, d1, d2, A0, A1);
-                if (guard)
-                    slide<Real, K, true>(ln_, E, k0, T, A0, A1, coef, o);
-                else
-                    slide<Real, K, false>(ln_, E, k0, T, A0, A1, coef, o);
-                chunk_partials<Real, K>(o, k0, E, r1, r2, S, Pr, Su);
-            }
+            if (a.scaled)
+                run_pass<Real, K, ES, PS, true>(ln, pp0, QS, E, nch, j, T, d1, d2, r1, r2, direct, cs, o, S, Pr, Su);
+            else
+                run_pass<Real, K, ES, PS, false>(ln, pp0, QS, E, nch, j, T, d1, d2, r1, r2, direct, cu, o, S, Pr,
+                                                 Su);
         }
         __syncthreads();
         if (active) {
+            const int k0 = j * K;
             if (k0 + K <= E) {
 #pragma unroll
                 for (int i = 0; i < K; i++)
-                    ln_[k0 + i] = o[i];
+                    ln[(k0 + i) * ES] = o[i];
             } else {
 #pragma unroll
                 for (int i = 0; i < K; i++)
                     if (k0 + i < E)
-                        ln_[k0 + i] = o[i];
+                        ln[(k0 + i) * ES] = o[i];
             }
             if (!direct) {
-                pp[j] = S;
-                pp[CP + j] = Pr;
-                pp[2 * CP + j] = Su;
+                pp[0] = S;
+                pp[QS] = Pr;
+                pp[2 * QS] = Su;
             }
         }
     }
@@ -425,50 +531,86 @@ __global__ void __launch_bounds__(1024, 1) k_axis(const AxisLaunch a, const Geom
 
     // ---- store ------------------------------------------------------------
     const int s0 = (int)(t0 - e0), s1 = (int)(t1 - e0);   // this tile's own cells
-    const int ns = s1 - s0;
-    if (a.store_quot) {
-        const Real thr = (Real)a.thr;
-        for (int idx = tid; idx < nl * ns; idx += blockDim.x) {
-            int ln, e;
-            if (a.axis == 0) {
-                ln = idx / ns;
-                e = s0 + idx % ns;
+    const Real thr = (Real)a.thr;
+    if (LAYOUT == 0) {
+        for (int q = 0; q < nl; q++) {
+            const Real *v_ = sm + (size_t)(q * 2) * P;
+            const Real *w_ = v_ + P;
+            const int64_t gb = (line0 + q) * a.L + e0;
+            if (a.store_quot) {
+                if (a.out_f64) {
+                    double *o_ = reinterpret_cast<double *>(a.out) + gb;
+                    for (int e = s0 + tid; e < s1; e += nthr)
+                        o_[e] = (double)quotient<Real>(v_[e], w_[e], thr, offset);
+                } else {
+                    float *o_ = reinterpret_cast<float *>(a.out) + gb;
+                    for (int e = s0 + tid; e < s1; e += nthr)
+                        o_[e] = (float)quotient<Real>(v_[e], w_[e], thr, offset);
+                }
             } else {
-                ln = idx % nl;
-                e = s0 + idx / nl;
-            }
-            const Real v = sm[(ln * 2 + 0) * P + e];
-            const Real w = sm[(ln * 2 + 1) * P + e];
-            const int64_t gi = line_base(a, g, line0 + ln) + (e0 + e) * a.elem_stride;
-            if (sizeof(Real) == 8) {
-                double q = (w < thr) ? __longlong_as_double(0x7ff8000000000000ll) : (double)v / (double)w + offset;
-                if (a.out_f64)
-                    reinterpret_cast<double *>(a.out)[gi] = q;
-                else
-                    reinterpret_cast<float *>(a.out)[gi] = (float)q;
-            } else {
-                float q = (w < thr) ? __int_as_float(0x7fc00000) : (float)v / (float)w + (float)offset;
-                if (a.out_f64)
-                    reinterpret_cast<double *>(a.out)[gi] = (double)q;
-                else
-                    reinterpret_cast<float *>(a.out)[gi] = q;
+                Real *dv = reinterpret_cast<Real *>(a.dst_v) + gb;
+                Real *dw = reinterpret_cast<Real *>(a.dst_w) + gb;
+                for (int e = s0 + tid; e < s1; e += nthr) {
+                    dv[e] = v_[e];
+                    dw[e] = w_[e];
+                }
             }
         }
     } else {
-        Real *dv = reinterpret_cast<Real *>(a.dst_v);
-        Real *dw = reinterpret_cast<Real *>(a.dst_w);
-        for (int idx = tid; idx < nl * ns; idx += blockDim.x) {
-            int ln, e;
-            if (a.axis == 0) {
-                ln = idx / ns;
-                e = s0 + idx % ns;
-            } else {
-                ln = idx % nl;
-                e = s0 + idx / nl;
+        const int64_t es = a.elem_stride;
+        const Real *v_ = sm;
+        const Real *w_ = sm + (size_t)P * G;
+        if (a.store_quot) {
+            // 4 cells of one row per thread: one 16-byte float32 store
+            const int nq = (s1 - s0) * (G / 4);
+            const bool q_vec = nl == G && !a.out_f64 && (gbase % 4) == 0 && (es % 4) == 0;
+            for (int i = tid; i < nq; i += nthr) {
+                const int row = s0 + i / (G / 4), c4 = (i % (G / 4)) * 4;
+                Real q4[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                    q4[u] = quotient<Real>(v_[row * G + c4 + u], w_[row * G + c4 + u], thr, offset);
+                const int64_t gi = gbase + row * es + c4;
+                if (q_vec) {
+                    *reinterpret_cast<float4 *>(reinterpret_cast<float *>(a.out) + gi) =
+                        make_float4((float)q4[0], (float)q4[1], (float)q4[2], (float)q4[3]);
+                } else {
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        if (c4 + u < nl) {
+                            if (a.out_f64)
+                                reinterpret_cast<double *>(a.out)[gi + u] = (double)q4[u];
+                            else
+                                reinterpret_cast<float *>(a.out)[gi + u] = (float)q4[u];
+                        }
+                    }
+                }
             }
-            const int64_t gi = line_base(a, g, line0 + ln) + (e0 + e) * a.elem_stride;
-            dv[gi] = sm[(ln * 2 + 0) * P + e];
-            dw[gi] = sm[(ln * 2 + 1) * P + e];
+        } else {
+            Real *dst[2] = {reinterpret_cast<Real *>(a.dst_v), reinterpret_cast<Real *>(a.dst_w)};
+            if (vec_ok) {
+                using V = typename Vec<G, Real>::T;
+                constexpr int VR = G / VPR;
+                const int nv = (s1 - s0) * VR;
+                for (int ff = 0; ff < 2; ff++) {
+                    const V *s_ = reinterpret_cast<const V *>(sm + (size_t)ff * P * G) + s0 * VR;
+                    Real *d_ = dst[ff] + gbase;
+                    for (int i = tid; i < nv; i += nthr) {
+                        const int row = s0 + i / VR, h = i - (row - s0) * VR;
+                        *reinterpret_cast<V *>(d_ + row * es + h * VPR) = s_[i];
+                    }
+                }
+            } else {
+                for (int ff = 0; ff < 2; ff++) {
+                    const Real *s_ = sm + (size_t)ff * P * G;
+                    Real *d_ = dst[ff] + gbase;
+                    for (int i = tid; i < (s1 - s0) * G; i += nthr) {
+                        const int row = s0 + i / G, gg = i % G;
+                        if (gg < nl)
+                            d_[row * es + gg] = s_[row * G + gg];
+                    }
+                }
+            }
         }
     }
 }
@@ -487,7 +629,9 @@ static int chunk_k(int precision, int T)
         return K64;
     return T <= 32 ? K64 : K32;
 }
+
 static int real_size(int precision) { return precision == 0 ? 8 : 4; }
+static int col_g(int precision) { return 32 / real_size(precision); }
 
 static size_t smem_limit()
 {
@@ -502,34 +646,53 @@ static size_t smem_limit()
     return (size_t)lim;
 }
 
-AxisPlanLimits axis_limits(int precision, int T)
-{
-    AxisPlanLimits l;
-    l.smem_limit = smem_limit();
-    const int K = chunk_k(precision, T), sz = real_size(precision);
-    // largest extent E with one line per CTA: threads and shared memory
-    // a line takes two thread groups (value, weight) of chunks_pad threads
-    int e_thr = kMaxLineThreads / 2 * K;
-    int lo = 1, hi = e_thr;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) / 2;
-        int nch = (mid + K - 1) / K;
-        int cp = (nch + 31) / 32 * 32;
-        size_t pitch = (size_t)(mid + 31) / 32 * 32 + 2;
-        size_t b = 2 * pitch * sz + 6 * (size_t)cp * sz;
-        if (2 * cp <= kMaxLineThreads && b <= l.smem_limit)
-            lo = mid;
-        else
-            hi = mid - 1;
-    }
-    l.extent_max = lo;
-    return l;
-}
+static int pitch_of(int64_t E) { return (int)((E + 31) / 32 * 32); }
 
 size_t axis_smem_bytes(int precision, const AxisLaunch &a)
 {
-    const int sz = real_size(precision);
-    return (size_t)a.lines_per_cta * (2 * (size_t)a.line_pitch * sz + 6 * (size_t)a.chunks_pad * sz);
+    const size_t sz = real_size(precision);
+    if (a.layout == 0)
+        return (size_t)a.lines_per_cta * (2 * (size_t)a.line_pitch + 6 * (size_t)a.chunks_pad) * sz;
+    const size_t G = col_g(precision);
+    return (2 * (size_t)a.line_pitch * G + 6 * (size_t)a.chunks_pad * G) * sz;
+}
+
+static int threads_of(int precision, const AxisLaunch &a)
+{
+    if (a.layout == 0)
+        return a.lines_per_cta * 2 * a.chunks_pad;
+    return 2 * col_g(precision) * a.chunks_pad;
+}
+
+AxisPlanLimits axis_limits(int precision, int T)
+{
+    // the longest extent a rows-layout CTA (one line) and a columns-layout CTA
+    // (G lines) can hold; the plan uses the one of its layout
+    AxisPlanLimits l;
+    l.smem_limit = smem_limit();
+    const int K = chunk_k(precision, T);
+    int best_rows = 0, best_cols = 0;
+    for (int lay = 0; lay < 2; lay++) {
+        int lo = 1, hi = kMaxLineThreads * K;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) / 2;
+            AxisLaunch a{};
+            a.layout = lay;
+            a.lines_per_cta = 1;
+            a.line_pitch = pitch_of(mid);
+            int nch = (mid + K - 1) / K;
+            int unit = lay == 0 ? 32 : 32 / col_g(precision);
+            a.chunks_pad = (nch + unit - 1) / unit * unit;
+            if (threads_of(precision, a) <= kMaxLineThreads && axis_smem_bytes(precision, a) <= l.smem_limit)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        (lay == 0 ? best_rows : best_cols) = lo;
+    }
+    l.extent_max = best_rows;
+    l.extent_max_cols = best_cols;
+    return l;
 }
 
 bool axis_shape(int precision, AxisLaunch &a)
@@ -539,55 +702,56 @@ bool axis_shape(int precision, AxisLaunch &a)
     if (E > a.L)
         E = a.L;
     const int nch = (int)((E + K - 1) / K);
-    const int cp = (nch + 31) / 32 * 32;
-    if (2 * cp > kMaxLineThreads)
-        return false;
+    const int unit = a.layout == 0 ? 32 : 32 / col_g(precision);
+    a.chunks_pad = (nch + unit - 1) / unit * unit;
     a.extent_max = (int)E;
-    a.chunks_pad = cp;
-    a.line_pitch = (int)((E + 31) / 32 * 32 + 2);
-    // lines per CTA: contiguous rows want ~256-512 threads; strided axes want
-    // 32-byte row segments (8 floats / 4 doubles) for sector-sized loads.
-    int want = a.axis == 0 ? std::max(1, 256 / cp) : (precision == 0 ? 4 : 8);
-    int nl = std::max(1, std::min<int>(want, kMaxLineThreads / (2 * cp)));
+    a.line_pitch = pitch_of(E);
+    if (a.layout == 1) {
+        a.lines_per_cta = col_g(precision);
+        return threads_of(precision, a) <= kMaxLineThreads && axis_smem_bytes(precision, a) <= smem_limit();
+    }
+    // rows: ~512 threads per CTA
+    int nl = std::max(1, std::min<int>(std::max(1, 256 / a.chunks_pad), kMaxLineThreads / (2 * a.chunks_pad)));
     if (nl > a.nlines)
         nl = (int)a.nlines;
-    while (nl > 1) {
+    for (; nl >= 1; nl--) {
         a.lines_per_cta = nl;
-        if (axis_smem_bytes(precision, a) <= smem_limit())
-            break;
-        nl--;
+        if (axis_smem_bytes(precision, a) <= smem_limit() && threads_of(precision, a) <= kMaxLineThreads)
+            return true;
     }
-    a.lines_per_cta = nl;
-    return axis_smem_bytes(precision, a) <= smem_limit();
+    return false;
 }
 
-template <typename Real, int K, int SD>
+template <typename Real, int K, int SD, int LAY>
 static cudaError_t launch_one(const AxisLaunch &a, const Geometry &g, const SampleView &sv, cudaStream_t st)
 {
-    const size_t smem = axis_smem_bytes(sizeof(Real) == 8 ? 0 : 1, a);
-    static size_t configured = 0;
-    if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_axis<Real, K, SD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    const int prec = sizeof(Real) == 8 ? 0 : 1;
+    const size_t smem = axis_smem_bytes(prec, a);
+    static bool configured = false;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(k_axis<Real, K, SD, LAY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem_limit());
         if (e != cudaSuccess)
             return e;
-        configured = smem_limit();
+        configured = true;
     }
-    const int64_t groups = (a.nlines + a.lines_per_cta - 1) / a.lines_per_cta;
+    const int64_t groups = a.layout == 0 ? (a.nlines + a.lines_per_cta - 1) / a.lines_per_cta
+                                         : a.outer_count * a.xblocks;
     const int64_t blocks = groups * a.ntiles;
-    const int threads = a.lines_per_cta * 2 * a.chunks_pad;
-    k_axis<Real, K, SD><<<(unsigned)blocks, threads, smem, st>>>(a, g, sv);
+    k_axis<Real, K, SD, LAY><<<(unsigned)blocks, threads_of(prec, a), smem, st>>>(a, g, sv);
     return cudaGetLastError();
 }
 
 template <typename Real, int K>
 static cudaError_t launch_k(int sd, const AxisLaunch &a, const Geometry &g, const SampleView &sv, cudaStream_t st)
 {
+    if (a.layout == 1)
+        return launch_one<Real, K, 0, 1>(a, g, sv, st);
     switch (sd) {
-    case 0: return launch_one<Real, K, 0>(a, g, sv, st);
-    case 1: return launch_one<Real, K, 1>(a, g, sv, st);
-    case 2: return launch_one<Real, K, 2>(a, g, sv, st);
-    default: return launch_one<Real, K, 3>(a, g, sv, st);
+    case 0: return launch_one<Real, K, 0, 0>(a, g, sv, st);
+    case 1: return launch_one<Real, K, 1, 0>(a, g, sv, st);
+    case 2: return launch_one<Real, K, 2, 0>(a, g, sv, st);
+    default: return launch_one<Real, K, 3, 0>(a, g, sv, st);
     }
 }
 
@@ -595,6 +759,8 @@ cudaError_t launch_axis(int precision, const AxisLaunch &a, const Geometry &g, c
                         cudaStream_t st)
 {
     const int sd = a.fill_splat ? g.dim : 0;
+    if (a.layout == 1 && a.fill_splat)
+        return cudaErrorInvalidValue;
     if (precision == 0)
         return launch_k<double, K64>(sd, a, g, sv, st);
     if (chunk_k(precision, a.T) == K64)
@@ -607,6 +773,7 @@ cudaError_t launch_lines(int precision, void *data, int64_t nlines, int64_t len,
 {
     AxisLaunch a{};
     a.axis = 0;
+    a.layout = 0;
     a.L = len;
     a.elem_stride = 1;
     a.nlines = nlines;
@@ -616,7 +783,8 @@ cudaError_t launch_lines(int precision, void *data, int64_t nlines, int64_t len,
     a.passes = passes;
     a.T = T;
     a.alpha = alpha;
-    a.inv_norm = normalize ? 1.0 / (2.0 * T + 1.0 + 2.0 * alpha) : 1.0;
+    a.scaled = normalize ? 1 : 0;
+    a.inv_norm = 1.0 / (2.0 * T + 1.0 + 2.0 * alpha);
     a.fill_splat = 0;
     a.store_quot = 0;
     a.src_v = data;

@@ -173,23 +173,37 @@ int make_plan(int method, int precision, int dim, int64_t npts, const double *si
         p.nbins = (uint32_t)(size[1] * size[2]);
     }
 
+    // float32 sums are left unscaled (like the reference's float64 ones)
+    // unless the kernel growth prod_m (2T+1+2a)^n could overflow float32
+    double growth = 1.0;
+    for (int m = 0; m < dim; m++)
+        growth *= pow(1.0 / inv[m], (double)num_iter);
+    const bool scaled = precision == FB_FP32C && growth * (double)std::max<int64_t>(npts, 1) > 1e24;
+
     // per-axis launches; `cur` tracks which buffer pair holds the data
     int cur = -1;   // -1: nothing yet (first launch splats)
     for (int m = 0; m < dim; m++) {
         const int64_t L = size[m];
         const int T = g.T[m];
         const AxisPlanLimits lim = axis_limits(precision, T);
+        const int64_t emax = m == 0 ? lim.extent_max : lim.extent_max_cols;
         std::vector<AxisLaunch> axl;
         AxisLaunch a{};
         a.axis = m;
+        a.layout = m == 0 ? 0 : 1;
         a.L = L;
         a.elem_stride = m == 0 ? 1 : (m == 1 ? size[0] : size[0] * size[1]);
         a.nlines = p.npoints / L;
+        a.width = size[0];
+        a.xblocks = (size[0] + (precision == FB_FP64 ? 4 : 8) - 1) / (precision == FB_FP64 ? 4 : 8);
+        a.outer_count = m == 1 ? (dim > 2 ? size[2] : 1) : (m == 2 ? size[1] : 1);
+        a.outer_stride = m == 1 ? size[0] * size[1] : size[0];
         a.T = T;
         a.alpha = g.alpha[m];
-        a.inv_norm = precision == FB_FP32C ? inv[m] : 1.0;
+        a.scaled = scaled ? 1 : 0;
+        a.inv_norm = inv[m];
         bool ok = false;
-        if (L <= lim.extent_max) {
+        if (L <= emax) {
             a.tile_len = L;
             a.ntiles = 1;
             a.halo = 0;
@@ -200,8 +214,8 @@ int make_plan(int method, int precision, int dim, int64_t npts, const double *si
         }
         if (!ok) {
             const int64_t h = (int64_t)num_iter * (T + 1);
-            const int64_t tl = lim.extent_max - 2 * h;
-            if (tl >= std::max<int64_t>(1024, lim.extent_max / 4)) {
+            const int64_t tl = emax - 2 * h;
+            if (tl >= std::max<int64_t>(1024, emax / 4)) {
                 a.tile_len = tl;
                 a.ntiles = (L + tl - 1) / tl;
                 a.halo = (int)h;
@@ -213,7 +227,7 @@ int make_plan(int method, int precision, int dim, int64_t npts, const double *si
         }
         if (!ok) {
             const int64_t h = T + 1;
-            const int64_t tl = lim.extent_max - 2 * h;
+            const int64_t tl = emax - 2 * h;
             if (tl >= 256) {
                 a.tile_len = tl;
                 a.ntiles = (L + tl - 1) / tl;
@@ -234,7 +248,7 @@ int make_plan(int method, int precision, int dim, int64_t npts, const double *si
             const bool last = (m == dim - 1) && (q + 1 == axl.size());
             x.fill_splat = first ? 1 : 0;
             x.store_quot = last ? 1 : 0;
-            x.thr = precision == FB_FP32C ? thr * scale : thr;
+            x.thr = scaled ? thr * scale : thr;
             int src = cur, dst;
             if (last)
                 dst = -2;

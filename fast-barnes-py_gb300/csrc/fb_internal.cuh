@@ -85,22 +85,34 @@ struct SampleView {
 };
 
 // One launch of the line-pass kernel along one axis.
+//
+// Rows layout (axis 0): lines are grid rows, contiguous in HBM; a CTA takes
+// lines_per_cta consecutive rows, each line buffer [e] in shared memory.
+// Columns layout (axes 1, 2): a CTA takes G adjacent lines (adjacent x, same
+// z for axis 1 / same y for axis 2), held interleaved [e][G] in shared memory,
+// so that one 32-byte row segment in HBM is one 32-byte row in shared memory.
 struct AxisLaunch {
-    int axis;                 // 0 = x (contiguous lines), 1 = y, 2 = z
+    int axis;                 // 0 = x, 1 = y, 2 = z
+    int layout;               // 0 = rows, 1 = columns
     int64_t L;                // line length
-    int64_t elem_stride;      // distance between consecutive line elements
-    int64_t nlines;           // lines along this axis
-    int lines_per_cta;        // lines processed together (adjacent lines)
+    int64_t elem_stride;      // HBM distance between consecutive cells of a line
+    int64_t nlines;           // rows layout: lines along this axis
+    int64_t outer_count;      // columns layout: planes (z for axis 1, y for axis 2)
+    int64_t outer_stride;     // columns layout: HBM distance between planes
+    int64_t xblocks;          // columns layout: groups of G lines per plane
+    int64_t width;            // columns layout: lines per plane (grid nx)
+    int lines_per_cta;        // rows: lines per CTA; columns: G
     int64_t tile_len;         // output positions per tile (== L if untiled)
     int64_t ntiles;           // tiles per line
     int halo;                 // extra input cells on each side of a tile
-    int extent_max;           // largest smem extent of one line
-    int line_pitch;           // smem words (Real) reserved per line buffer
-    int chunks_pad;           // threads per line (chunks rounded up to 32)
+    int extent_max;           // largest shared-memory extent of one line
+    int line_pitch;           // shared-memory cells reserved per line
+    int chunks_pad;           // chunk slots per line (threads per line and field)
     int passes;               // box passes run in this launch
     int T;
     double alpha;
-    double inv_norm;          // 1/(2T+1+2alpha) for the scaled fp32 form, else 1
+    int scaled;               // 1: every pass is multiplied by inv_norm
+    double inv_norm;          // 1/(2T+1+2alpha)
     int fill_splat;           // 1: fill by splatting samples, 0: load from src
     int store_quot;           // 1: last axis -> quotient + mask + offset
     int out_f64;              // quotient output type: 1 = float64, 0 = float32

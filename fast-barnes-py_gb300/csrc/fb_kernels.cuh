@@ -12,8 +12,9 @@ cudaError_t sort_samples(const double *pts, const double *val, int64_t npts, con
 
 // fb_axis.cu
 struct AxisPlanLimits {
-    int extent_max;      // longest line extent held in shared memory
-    size_t smem_limit;   // dynamic shared memory per block
+    int extent_max;        // longest line extent a rows-layout CTA holds
+    int extent_max_cols;   // longest line extent a columns-layout CTA holds
+    size_t smem_limit;     // dynamic shared memory per block
 };
 // Longest line extent one CTA holds for half kernel width T.
 AxisPlanLimits axis_limits(int precision, int T);
