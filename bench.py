@@ -269,7 +269,7 @@ def main():
     for i in range(nrec.value):
         per_stage.setdefault(stages[i], []).append(times[i])
     sz = 4 if prec == _lib.FB_FP32C else 8
-    alg = {0: NPTS * (24 + 16 * 4),                          # sort: coords+value read, keys/idx passes
+    alg = {0: NPTS * (24 + 4 * 6),                           # sort: coords+value read, keys / indices
            1: NPTS * 28 + W * H * 2 * sz,                    # splat + row passes: samples in, v,w out
            2: W * H * 2 * sz + W * H * 4}                    # column passes + quotient: v,w in, float32 out
     names = {0: "sample sort", 1: "k_axis x-passes (splat fused)", 2: "k_axis y-passes (quotient fused)"}
@@ -345,10 +345,8 @@ def main():
         cpu = {"value": rate, "unit": "Mgridpts/s", "cores": 1, "kind": "port",
                "sample": f"{nf} field(s) of {W}x{H}, N={NPTS}, float64, single thread, {secs:.1f} s"}
 
-    launches_per_field = 0
-    # header init, bin keys, per radix pass (hist, scan, scatter), bin starts, two axis launches
-    radix_passes = (int(math.log2(H)) + 1 + 7) // 8
-    launches_per_field = 1 + 1 + 3 * radix_passes + 1 + 2
+    # bin keys, scan, bin scatter, bin sort, large-bin sort, two axis launches
+    launches_per_field = 5 + 2
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "Mgridpts/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,

@@ -278,7 +278,7 @@ int make_plan(int method, int precision, int dim, int64_t npts, const double *si
     p.off_bins = off;
     off = align_up(off + sizeof(uint32_t) * ((size_t)p.nbins + 1));
     p.off_sort = off;
-    off = align_up(off + sort_scratch_bytes(npts));
+    off = align_up(off + sort_scratch_bytes(npts, p.nbins));
     for (int q = 0; q < p.pairs; q++) {
         p.off_pair[q] = off;
         off = align_up(off + 2 * sz * (size_t)p.npoints);
@@ -296,11 +296,12 @@ void resolve_pointers(const Plan &p, char *ws, void *out, AxisLaunch &a)
             return nullptr;
         return ws + p.off_pair[idx] + (size_t)f * sz * (size_t)p.npoints;
     };
+    // intermediate fields are interleaved (v, w) cells: one buffer per pair
     intptr_t s = (intptr_t)a.src_v, d = (intptr_t)a.dst_v;
     a.src_v = pair(s, 0);
-    a.src_w = pair(s, 1);
+    a.src_w = nullptr;
     a.dst_v = pair(d, 0);
-    a.dst_w = pair(d, 1);
+    a.dst_w = nullptr;
     a.out = out;
 }
 

@@ -21,8 +21,10 @@ constexpr int K64 = 17;   // float64 form (8-byte words: half-warp phases)
 constexpr int kMaxLineThreads = 1024;
 
 // Per-field scalars written on the device (min/max of the values, flags).
+// All fields start at zero; the minimum is kept complemented so that an
+// atomic maximum on a zeroed word computes it.
 struct FieldHeader {
-    unsigned long long vmin_key;   // ordered-integer encoding of min(val)
+    unsigned long long vmin_key;   // complemented ordered-integer encoding of min(val)
     unsigned long long vmax_key;   // ordered-integer encoding of max(val)
     int nan_seen;                  // any NaN in val -> offset is NaN
     int error;                     // device-side error word (0 = ok)
@@ -58,7 +60,7 @@ __device__ inline double field_offset(const FieldHeader *h)
 {
     if (h->nan_seen)
         return __longlong_as_double(0x7ff8000000000000ll);
-    return (ordered_to_dbl(h->vmin_key) + ordered_to_dbl(h->vmax_key)) / 2.0;
+    return (ordered_to_dbl(~h->vmin_key) + ordered_to_dbl(h->vmax_key)) / 2.0;
 }
 
 // Geometry and parameters of one interpolation, shared by all kernels.
@@ -116,6 +118,7 @@ struct AxisLaunch {
     int fill_splat;           // 1: fill by splatting samples, 0: load from src
     int store_quot;           // 1: last axis -> quotient + mask + offset
     int out_f64;              // quotient output type: 1 = float64, 0 = float32
+    int plain;                // rows layout: src / dst are single-field Real lines
     double thr;               // mask level in the units of the stored weights
     const void *src_v, *src_w;
     void *dst_v, *dst_w;

@@ -5,7 +5,7 @@
 namespace fbg {
 
 // fb_sort.cu
-size_t sort_scratch_bytes(int64_t npts);
+size_t sort_scratch_bytes(int64_t npts, uint32_t nbins);
 cudaError_t sort_samples(const double *pts, const double *val, int64_t npts, const Geometry &g,
                          int bin_w, uint32_t nbins, FieldHeader *hdr, uint32_t *scratch,
                          uint32_t *bin_start, const uint32_t **sorted_idx, cudaStream_t st);

@@ -1,35 +1,29 @@
 // fb_sort.cu -- sample preparation for the splat: value range, bin keys and a
-// stable, deterministic counting sort of the samples by grid row.
+// deterministic ordering of the samples by grid row.
 //
 // Replaces the per-sample loop head of _inject_data_{1,2,3}d
 // (fastbarnes/interpolation.py:218-322: cell index, skip rule) and
-// _normalize_values (:204-212: min/max of the values).  The reference adds the
-// samples in index order; the splatting kernel keeps that order inside every
-// row because the sort below is stable (LSD radix sort, 8-bit digits, ranks
-// resolved warp-serially in index order).
+// _normalize_values (:204-212: min/max of the values).
+//
+// Samples are counted per bin (grid row, or (z, y) row, or x range in 1D),
+// the counts are scanned into bin starts, every sample is placed into its bin
+// with an atomic cursor, and finally every bin is sorted by sample index, so
+// the order inside a bin is the samples' own order whatever the atomics did.
+// The splatting kernel then adds each row's samples in that order.
+#include <algorithm>
+
 #include "fb_internal.cuh"
 #include "fb_kernels.cuh"
 
 namespace fbg {
 
-constexpr int kSortItems = 64;                  // keys per lane per tile
-constexpr int kSortTile = 32 * kSortItems;      // keys per warp tile
-constexpr int kSortWarps = 4;                   // warps (tiles) per block
-
-__global__ void k_header_init(FieldHeader *h)
-{
-    h->vmin_key = ~0ull;
-    h->vmax_key = 0ull;
-    h->nan_seen = 0;
-    h->error = 0;
-}
-
-// Bin key of every sample (nbins for samples the reference skips) and the
-// min / max / NaN reduction of the values.
+// Bin key of every sample (nbins for samples the reference skips), the count
+// of every bin, and the min / max / NaN reduction of the values.  The header
+// and the counts start zeroed (min is kept complemented for that reason).
 template <int DIM>
 __global__ void k_bin_keys(const double *__restrict__ pts, const double *__restrict__ val, int64_t npts,
                            Geometry g, int bin_w, uint32_t nbins, uint32_t *__restrict__ keys,
-                           FieldHeader *hdr)
+                           uint32_t *__restrict__ counts, FieldHeader *hdr)
 {
     unsigned long long kmin = ~0ull, kmax = 0ull;
     int nan = 0;
@@ -61,6 +55,8 @@ __global__ void k_bin_keys(const double *__restrict__ pts, const double *__restr
                 key = (uint32_t)((int64_t)zc * g.size[1] + (int64_t)yc);
         }
         keys[k] = key;
+        if (key < nbins)
+            atomicAdd(&counts[key], 1u);
     }
     for (int o = 16; o > 0; o >>= 1) {
         unsigned long long a = __shfl_xor_sync(0xffffffffu, kmin, o);
@@ -71,7 +67,7 @@ __global__ void k_bin_keys(const double *__restrict__ pts, const double *__restr
     nan = __any_sync(0xffffffffu, nan);
     if ((threadIdx.x & 31) == 0) {
         if (kmin != ~0ull)
-            atomicMin(&hdr->vmin_key, kmin);
+            atomicMax(&hdr->vmin_key, ~kmin);
         if (kmax != 0ull)
             atomicMax(&hdr->vmax_key, kmax);
         if (nan)
@@ -79,161 +75,219 @@ __global__ void k_bin_keys(const double *__restrict__ pts, const double *__restr
     }
 }
 
-// Per-warp-tile histogram of one 8-bit digit, stored digit-major:
-// hist[d * ntiles + tile].
-__global__ void k_radix_hist(const uint32_t *__restrict__ keys, int64_t n, int shift,
-                             uint32_t *__restrict__ hist, int64_t ntiles)
+// Exclusive prefix sum of n entries, one block of 1024 threads walking tiles
+// of 4096 entries.
+__global__ void __launch_bounds__(1024) k_scan_exclusive(const uint32_t *__restrict__ in, uint32_t *__restrict__ out,
+                                                         int64_t n)
 {
-    __shared__ uint32_t cnt[kSortWarps][256];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t tile = (int64_t)blockIdx.x * kSortWarps + w;
-    for (int d = lane; d < 256; d += 32)
-        cnt[w][d] = 0;
-    __syncwarp();
-    if (tile < ntiles) {
-        const int64_t base = tile * kSortTile;
-        for (int s = 0; s < kSortItems; s++) {
-            int64_t i = base + s * 32 + lane;
+    __shared__ uint32_t wsum[32];
+    __shared__ uint32_t carry_s;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    uint32_t carry = 0;
+    for (int64_t base = 0; base < n; base += 4096) {
+        uint32_t x[4];
+        uint32_t s = 0;
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int64_t i = base + 4 * t + u;
+            x[u] = i < n ? in[i] : 0u;
+            s += x[u];
+        }
+        // inclusive scan of the thread sums
+        uint32_t inc = s;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o)
+                inc += y;
+        }
+        if (lane == 31)
+            wsum[w] = inc;
+        __syncthreads();
+        if (w == 0) {
+            uint32_t ws = wsum[lane];
+            uint32_t wi = ws;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
+                if (lane >= o)
+                    wi += y;
+            }
+            wsum[lane] = wi - ws;   // exclusive warp offsets
+            if (lane == 31)
+                carry_s = wi;
+        }
+        __syncthreads();
+        uint32_t run = carry + wsum[w] + inc - s;
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int64_t i = base + 4 * t + u;
             if (i < n)
-                atomicAdd(&cnt[w][(keys[i] >> shift) & 255u], 1u);
+                out[i] = run;
+            run += x[u];
         }
-        __syncwarp();
-        for (int d = lane; d < 256; d += 32)
-            hist[(int64_t)d * ntiles + tile] = cnt[w][d];
+        carry += carry_s;
+        __syncthreads();
     }
 }
 
-// Exclusive prefix sum of n entries in place, one block of 1024 threads.
-__global__ void k_scan_exclusive(uint32_t *data, int64_t n)
+// Places every sample into its bin; the order inside a bin is fixed later.
+__global__ void k_bin_scatter(const uint32_t *__restrict__ keys, int64_t npts, uint32_t nbins,
+                              const uint32_t *__restrict__ start, uint32_t *__restrict__ cursor,
+                              uint32_t *__restrict__ sorted)
 {
-    __shared__ uint32_t part[1024];
-    const int t = threadIdx.x;
-    const int64_t per = (n + 1023) / 1024;
-    const int64_t b = t * per, e = b + per < n ? b + per : n;
-    uint32_t s = 0;
-    for (int64_t i = b; i < e; i++)
-        s += data[i];
-    part[t] = s;
-    __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {
-        uint32_t v = t >= o ? part[t - o] : 0u;
-        __syncthreads();
-        part[t] += v;
-        __syncthreads();
-    }
-    uint32_t run = part[t] - s;
-    for (int64_t i = b; i < e; i++) {
-        uint32_t x = data[i];
-        data[i] = run;
-        run += x;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < npts;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t key = keys[k];
+        if (key < nbins)
+            sorted[start[key] + atomicAdd(&cursor[key], 1u)] = (uint32_t)k;
     }
 }
 
-// Stable scatter of one digit: inside a warp tile the keys are ranked in index
-// order, 32 at a time; lanes with equal digits are ranked by lane.
-__global__ void k_radix_scatter(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin,
-                                uint32_t *__restrict__ kout, uint32_t *__restrict__ vout, int64_t n,
-                                int shift, const uint32_t *__restrict__ offs, int64_t ntiles,
-                                int first)
+constexpr int kWarpSortMax = 1024;   // bins up to this size are sorted by one warp
+constexpr int kBinSortWarps = 8;
+
+struct WarpSync {
+    __device__ void operator()() const { __syncwarp(); }
+};
+struct BlockSync {
+    __device__ void operator()() const { __syncthreads(); }
+};
+
+// Bitonic compare-exchange network over n (a power of two) keys in shared
+// memory, threads [0, nthr) cooperating; `sync` orders the steps.
+template <typename Sync>
+__device__ __forceinline__ void bitonic(uint32_t *s, int n, int t, int nthr, Sync sync)
 {
-    __shared__ uint32_t cur[kSortWarps][256];
+    for (int k = 2; k <= n; k <<= 1) {
+        for (int jj = k >> 1; jj > 0; jj >>= 1) {
+            for (int i = t; i < n / 2; i += nthr) {
+                const int lo = ((i & ~(jj - 1)) << 1) | (i & (jj - 1));
+                const int hi = lo + jj;
+                const bool asc = (lo & k) == 0;
+                const uint32_t a = s[lo], b = s[hi];
+                if ((a > b) == asc) {
+                    s[lo] = b;
+                    s[hi] = a;
+                }
+            }
+            sync();
+        }
+    }
+}
+
+// Sorts every bin's entries by sample index: one warp per bin, in registers for
+// up to 32 entries, in shared memory up to kWarpSortMax; larger bins are listed
+// for k_sort_large.
+__global__ void __launch_bounds__(32 * kBinSortWarps) k_sort_bins(const uint32_t *__restrict__ start, uint32_t nbins,
+                                                                  uint32_t *__restrict__ sorted,
+                                                                  uint32_t *__restrict__ large)
+{
+    __shared__ uint32_t buf[kBinSortWarps][kWarpSortMax];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t tile = (int64_t)blockIdx.x * kSortWarps + w;
-    if (tile >= ntiles)
+    const int64_t b = (int64_t)blockIdx.x * kBinSortWarps + w;
+    if (b >= nbins)
         return;
-    for (int d = lane; d < 256; d += 32)
-        cur[w][d] = offs[(int64_t)d * ntiles + tile];
-    __syncwarp();
-    const uint32_t lt = (1u << lane) - 1u;
-    const int64_t base = tile * kSortTile;
-    for (int s = 0; s < kSortItems; s++) {
-        int64_t i = base + s * 32 + lane;
-        bool valid = i < n;
-        uint32_t key = valid ? kin[i] : 0u;
-        uint32_t v = valid ? (first ? (uint32_t)i : vin[i]) : 0u;
-        uint32_t d = valid ? ((key >> shift) & 255u) : 256u;
-        uint32_t peers = __match_any_sync(0xffffffffu, d);
-        uint32_t rank = __popc(peers & lt);
-        uint32_t pos = valid ? cur[w][d] + rank : 0u;
-        __syncwarp();
-        if (valid && lane == 31 - __clz(peers))
-            cur[w][d] += __popc(peers);
-        __syncwarp();
-        if (valid) {
-            kout[pos] = key;
-            vout[pos] = v;
+    const uint32_t s0 = start[b], c = start[b + 1] - s0;
+    if (c <= 1)
+        return;
+    if (c <= 32) {
+        uint32_t x = lane < (int)c ? sorted[s0 + lane] : 0xFFFFFFFFu;
+        for (int k = 2; k <= 32; k <<= 1) {
+            for (int jj = k >> 1; jj > 0; jj >>= 1) {
+                const uint32_t y = __shfl_xor_sync(0xffffffffu, x, jj);
+                const bool asc = (lane & k) == 0;
+                const bool lower = (lane & jj) == 0;
+                x = (lower == asc) ? min(x, y) : max(x, y);
+            }
         }
-    }
-}
-
-// bin_start[b] = first sorted position whose key is >= b, b in [0, nbins].
-__global__ void k_bin_start(const uint32_t *__restrict__ skeys, int64_t n, uint32_t *__restrict__ start,
-                            uint32_t nbins)
-{
-    int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (b > nbins)
+        if (lane < (int)c)
+            sorted[s0 + lane] = x;
         return;
-    int64_t lo = 0, hi = n;
-    while (lo < hi) {
-        int64_t mid = (lo + hi) >> 1;
-        if (skeys[mid] < (uint32_t)b)
-            lo = mid + 1;
-        else
-            hi = mid;
     }
-    start[b] = (uint32_t)lo;
+    if (c <= kWarpSortMax) {
+        int n = 64;
+        while (n < (int)c)
+            n <<= 1;
+        uint32_t *s = buf[w];
+        for (int i = lane; i < n; i += 32)
+            s[i] = i < (int)c ? sorted[s0 + i] : 0xFFFFFFFFu;
+        __syncwarp();
+        bitonic(s, n, lane, 32, WarpSync());
+        for (int i = lane; i < (int)c; i += 32)
+            sorted[s0 + i] = s[i];
+        return;
+    }
+    if (lane == 0) {
+        const uint32_t slot = atomicAdd(&large[0], 1u);
+        large[1 + slot] = (uint32_t)b;
+    }
 }
 
-size_t sort_scratch_bytes(int64_t npts)
+// Sorts the bins too large for one warp, one block per bin at a time, in a
+// scratch area of twice the bin size (padded to a power of two with keys that
+// sort last).
+__global__ void __launch_bounds__(1024) k_sort_large(const uint32_t *__restrict__ start, uint32_t *__restrict__ sorted,
+                                                     const uint32_t *__restrict__ large,
+                                                     uint32_t *__restrict__ scratch)
 {
-    int64_t ntiles = (npts + kSortTile - 1) / kSortTile;
-    if (ntiles < 1)
-        ntiles = 1;
-    return (size_t)4 * (4 * (size_t)npts + 256 * (size_t)ntiles) + 256;
+    const uint32_t nlarge = large[0];
+    for (uint32_t q = blockIdx.x; q < nlarge; q += gridDim.x) {
+        const uint32_t b = large[1 + q];
+        const uint32_t s0 = start[b], c = start[b + 1] - s0;
+        int n = 1;
+        while (n < (int)c)
+            n <<= 1;
+        uint32_t *s = scratch + 2 * (size_t)s0;   // 2c >= n cells of this bin's own region
+        for (int i = threadIdx.x; i < n; i += blockDim.x)
+            s[i] = i < (int)c ? sorted[s0 + i] : 0xFFFFFFFFu;
+        __syncthreads();
+        bitonic(s, n, threadIdx.x, (int)blockDim.x, BlockSync());
+        for (int i = threadIdx.x; i < (int)c; i += blockDim.x)
+            sorted[s0 + i] = s[i];
+        __syncthreads();
+    }
 }
 
-// Orders the samples of one field by bin.  Scratch layout (uint32):
-// keys[N] | keys_alt[N] | idx[N] | idx_alt[N] | hist[256 * ntiles].
-cudaError_t sort_samples(const double *pts, const double *val, int64_t npts, const Geometry &g,
-                         int bin_w, uint32_t nbins, FieldHeader *hdr, uint32_t *scratch,
-                         uint32_t *bin_start, const uint32_t **sorted_idx, cudaStream_t st)
+// Scratch layout (uint32): counts[nbins + 1] | cursor[nbins + 1] |
+// large[nbins + 2] | keys[N] | sorted[N] | big-bin scratch[2N].
+size_t sort_scratch_bytes(int64_t npts, uint32_t nbins)
 {
-    k_header_init<<<1, 1, 0, st>>>(hdr);
-    int64_t ntiles = (npts + kSortTile - 1) / kSortTile;
-    uint32_t *keys = scratch, *keys2 = scratch + npts, *idx = scratch + 2 * npts, *idx2 = scratch + 3 * npts;
-    uint32_t *hist = scratch + 4 * npts;
+    return 4 * (3 * ((size_t)nbins + 2) + 4 * (size_t)npts) + 256;
+}
+
+cudaError_t sort_samples(const double *pts, const double *val, int64_t npts, const Geometry &g, int bin_w,
+                         uint32_t nbins, FieldHeader *hdr, uint32_t *scratch, uint32_t *bin_start,
+                         const uint32_t **sorted_idx, cudaStream_t st)
+{
+    uint32_t *counts = scratch;
+    uint32_t *cursor = counts + (nbins + 2);
+    uint32_t *large = cursor + (nbins + 2);
+    uint32_t *keys = large + (nbins + 2);
+    uint32_t *sorted = keys + npts;
+    uint32_t *big = sorted + npts;
+    cudaError_t e = cudaMemsetAsync(hdr, 0, sizeof(FieldHeader), st);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(counts, 0, sizeof(uint32_t) * 3 * ((size_t)nbins + 2), st);
+    if (e != cudaSuccess)
+        return e;
+    *sorted_idx = sorted;
     if (npts > 0) {
-        int blocks = (int)((npts + 255) / 256);
-        if (blocks > 152 * 16)
-            blocks = 152 * 16;
+        int blocks = (int)std::min<int64_t>((npts + 255) / 256, 152 * 8);
         if (g.dim == 1)
-            k_bin_keys<1><<<blocks, 256, 0, st>>>(pts, val, npts, g, bin_w, nbins, keys, hdr);
+            k_bin_keys<1><<<blocks, 256, 0, st>>>(pts, val, npts, g, bin_w, nbins, keys, counts, hdr);
         else if (g.dim == 2)
-            k_bin_keys<2><<<blocks, 256, 0, st>>>(pts, val, npts, g, bin_w, nbins, keys, hdr);
+            k_bin_keys<2><<<blocks, 256, 0, st>>>(pts, val, npts, g, bin_w, nbins, keys, counts, hdr);
         else
-            k_bin_keys<3><<<blocks, 256, 0, st>>>(pts, val, npts, g, bin_w, nbins, keys, hdr);
-        int bits = 32 - __builtin_clz(nbins | 1u);
-        int passes = (bits + 7) / 8;
-        int sblocks = (int)((ntiles + kSortWarps - 1) / kSortWarps);
-        const uint32_t *ki = keys, *vi = nullptr;
-        uint32_t *ko = keys2, *vo = idx;
-        for (int p = 0; p < passes; p++) {
-            k_radix_hist<<<sblocks, 32 * kSortWarps, 0, st>>>(ki, npts, 8 * p, hist, ntiles);
-            k_scan_exclusive<<<1, 1024, 0, st>>>(hist, 256 * ntiles);
-            k_radix_scatter<<<sblocks, 32 * kSortWarps, 0, st>>>(ki, vi, ko, vo, npts, 8 * p, hist, ntiles,
-                                                                p == 0);
-            // next pass reads what this one wrote
-            const uint32_t *nk = ko, *nv = vo;
-            ko = (ko == keys2) ? keys : keys2;
-            vo = (vo == idx) ? idx2 : idx;
-            ki = nk;
-            vi = nv;
-        }
-        *sorted_idx = vi;
-        k_bin_start<<<(int)((nbins + 1 + 255) / 256), 256, 0, st>>>(ki, npts, bin_start, nbins);
-    } else {
-        *sorted_idx = idx;
-        cudaMemsetAsync(bin_start, 0, sizeof(uint32_t) * (nbins + 1), st);
+            k_bin_keys<3><<<blocks, 256, 0, st>>>(pts, val, npts, g, bin_w, nbins, keys, counts, hdr);
+    }
+    k_scan_exclusive<<<1, 1024, 0, st>>>(counts, bin_start, (int64_t)nbins + 1);
+    if (npts > 0) {
+        int blocks = (int)std::min<int64_t>((npts + 255) / 256, 152 * 8);
+        k_bin_scatter<<<blocks, 256, 0, st>>>(keys, npts, nbins, bin_start, cursor, sorted);
+        k_sort_bins<<<(unsigned)((nbins + kBinSortWarps - 1) / kBinSortWarps), 32 * kBinSortWarps, 0, st>>>(
+            bin_start, nbins, sorted, large);
+        k_sort_large<<<64, 1024, 0, st>>>(bin_start, sorted, large, big);
     }
     return cudaGetLastError();
 }
