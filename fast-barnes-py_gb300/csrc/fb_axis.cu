@@ -785,7 +785,8 @@ static size_t smem_limit()
         cudaGetDevice(&dev);
         if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess || v <= 0)
             v = 227 * 1024;
-        lim = v;
+        // keep room for the kernels' few bytes of static shared memory
+        lim = v - 1024;
     }
     return (size_t)lim;
 }
