@@ -775,6 +775,7 @@ static int chunk_k(int precision, int T)
 
 static int cell_size(int precision) { return precision == 0 ? 16 : 8; }
 static int col_g(int precision) { return 32 / cell_size(precision); }
+int axis_col_group(int precision) { return col_g(precision); }
 constexpr int kMaxThreads = 512;
 
 static size_t smem_limit()

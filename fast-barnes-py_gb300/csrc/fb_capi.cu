@@ -195,7 +195,7 @@ int make_plan(int method, int precision, int dim, int64_t npts, const double *si
         a.elem_stride = m == 0 ? 1 : (m == 1 ? size[0] : size[0] * size[1]);
         a.nlines = p.npoints / L;
         a.width = size[0];
-        a.xblocks = (size[0] + (precision == FB_FP64 ? 4 : 8) - 1) / (precision == FB_FP64 ? 4 : 8);
+        a.xblocks = (size[0] + axis_col_group(precision) - 1) / axis_col_group(precision);
         a.outer_count = m == 1 ? (dim > 2 ? size[2] : 1) : (m == 2 ? size[1] : 1);
         a.outer_stride = m == 1 ? size[0] * size[1] : size[0];
         a.T = T;

@@ -18,6 +18,8 @@ struct AxisPlanLimits {
 };
 // Longest line extent one CTA holds for half kernel width T.
 AxisPlanLimits axis_limits(int precision, int T);
+// Lines per columns-layout CTA: 32 bytes of (v, w) cells per grid row.
+int axis_col_group(int precision);
 // Shared memory needed by one CTA of a launch.
 size_t axis_smem_bytes(int precision, const AxisLaunch &a);
 // Fills in lines_per_cta, extent_max, line_pitch, chunks_pad for a launch
