@@ -188,6 +188,7 @@ def main():
     ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--chunk", type=int, default=0, help="fb_tune chunk knob (0 automatic, 17, 33)")
     ap.add_argument("--quick", action="store_true",
                     help="warm-up and timed steps only (no fp64 form, e2e or CPU baseline): for profiler runs")
     args = ap.parse_args()
@@ -208,6 +209,7 @@ def main():
         torch.cuda.set_device(0)
     dev = torch.device("cuda", torch.cuda.current_device())
     L = _lib.lib()
+    _lib.check(L.fb_tune(b"chunk", args.chunk), "fb_tune")
     prec = _lib.PRECISIONS[args.precision]
     B = args.batch
 

@@ -1,762 +1,13 @@
-// fb_axis.cu -- the n-fold box-and-tail convolution along one grid axis.
-//
-// Replaces _convolve_tail_{1,2,3}d / _accumulate_tail_array
-// (fastbarnes/interpolation.py:372-533) and, for the first axis, the splat of
-// _inject_data_{1,2,3}d (:218-322); for the last axis it also applies the NaN
-// mask (:420-430) and the quotient (vg / wg + offset) of :367.
-//
-// The value and the weight field travel together as one cell (v, w): a float2
-// in the float32 form, whose two halves every pass updates with one packed
-// instruction (add/fma .f32x2), or a double2 in the float64 form.  Cells are
-// interleaved the same way in HBM between axes.
-//
-// One CTA holds whole lines (or halo-extended tiles of long lines) in shared
-// memory and runs all `passes` box passes there, so every grid point crosses
-// HBM once per axis.  Rows layout (axis 0): lines_per_cta consecutive rows,
-// line buffers [e].  Columns layout (axes 1, 2): G adjacent lines interleaved
-// [e][G], G cells = 32 bytes, so one 32-byte sector of a grid row is one row of
-// the CTA's buffer and loads / stores are plain 16-byte vector copies.
-//
-// Inside a pass every thread owns a chunk of K consecutive cells of one line.
-// It starts from the exact window sums at both chunk ends (anchors, summed
-// from per-chunk partial sums of the previous pass that lie entirely inside
-// the window, so nothing cancels), slides forward over the first half of the
-// chunk and backward over the second half, keeps the K outputs in registers,
-// and writes them back in place after a barrier.  K is odd, so the lanes of a
-// warp (consecutive chunks) spread over all banks.  Narrow kernels sum every
-// output directly from registers instead.
-//
-// Window semantics are the reference's (interpolation.py:500-523): out[k] =
-// sum_{|d|<=T} in[k+d] + alpha * (in[k-T-1] + in[k+T+1]), in[] = 0 outside
-// [0, L).  Inside a tile the region beyond the tile's input extent reads as 0
-// too; the halo of passes*(T+1) cells absorbs that, and only the tile's own
-// cells are stored.
+// fb_axis.cu -- launch shapes of the axis kernels (shared-memory extents,
+// threads, lines per CTA) and the dispatch to the per-precision instantiations
+// in fb_axis_f32.cu and fb_axis_f64.cu.
+#include <string.h>
+
 #include <algorithm>
 
-#include "fb_internal.cuh"
-#include "fb_kernels.cuh"
+#include "fb_axis_impl.cuh"
 
 namespace fbg {
-
-// ---------------------------------------------------------------------------
-// (v, w) cells and their arithmetic
-// ---------------------------------------------------------------------------
-
-template <typename Real>
-struct CellOf;
-template <>
-struct CellOf<float> {
-    using T = float2;
-};
-template <>
-struct CellOf<double> {
-    using T = double2;
-};
-
-__device__ __forceinline__ unsigned long long pk(float2 a)
-{
-    unsigned long long r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
-    return r;
-}
-__device__ __forceinline__ float2 upk(unsigned long long r)
-{
-    float2 a;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
-    return a;
-}
-
-__device__ __forceinline__ float2 cadd(float2 a, float2 b)
-{
-    unsigned long long d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)));
-    return upk(d);
-}
-__device__ __forceinline__ float2 csub(float2 a, float2 b)
-{
-    unsigned long long d;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)));
-    return upk(d);
-}
-__device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c)
-{
-    unsigned long long d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)), "l"(pk(c)));
-    return upk(d);
-}
-__device__ __forceinline__ float2 cmul(float2 a, float2 b)
-{
-    unsigned long long d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)));
-    return upk(d);
-}
-__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
-__device__ __forceinline__ double2 cfma(double2 a, double2 b, double2 c)
-{
-    return make_double2(fma(a.x, b.x, c.x), fma(a.y, b.y, c.y));
-}
-__device__ __forceinline__ double2 cmul(double2 a, double2 b) { return make_double2(a.x * b.x, a.y * b.y); }
-
-template <typename C>
-__device__ __forceinline__ C czero();
-template <>
-__device__ __forceinline__ float2 czero<float2>() { return make_float2(0.f, 0.f); }
-template <>
-__device__ __forceinline__ double2 czero<double2>() { return make_double2(0.0, 0.0); }
-
-template <typename C>
-__device__ __forceinline__ C csplat(double x);
-template <>
-__device__ __forceinline__ float2 csplat<float2>(double x) { return make_float2((float)x, (float)x); }
-template <>
-__device__ __forceinline__ double2 csplat<double2>(double x) { return make_double2(x, x); }
-
-// ---------------------------------------------------------------------------
-// one line seen by one thread: cell e lives at s[e * ES]
-// ---------------------------------------------------------------------------
-
-template <bool GUARD, int ES, typename C>
-__device__ __forceinline__ C rd(const C *__restrict__ s, int e, int E)
-{
-    if (GUARD)
-        return (unsigned)e < (unsigned)E ? s[e * ES] : czero<C>();
-    return s[e * ES];
-}
-
-template <typename C, bool SCALED>
-struct PassCoef {
-    C alpha;   // tail weight (alpha * inv when scaled), both halves
-    C inv;     // 1 / (2T+1+2alpha), both halves
-    __device__ __forceinline__ C out(C acc, C tails) const
-    {
-        if (SCALED)
-            return cfma(acc, inv, cmul(alpha, tails));
-        return cfma(alpha, tails, acc);
-    }
-};
-
-// Slides the window over the chunk [k0, k0 + K): forward from A0 (window at
-// k0) over the first half, backward from A1 (window at k0 + K) over the rest.
-template <typename C, int K, int ES, bool GUARD, bool SCALED>
-__device__ __forceinline__ void slide(const C *__restrict__ s, int E, int k0, int T, C A0, C A1,
-                                      const PassCoef<C, SCALED> &c, C (&o)[K])
-{
-    constexpr int H = K / 2;
-    C acc = A0;
-    C prev = rd<GUARD, ES>(s, k0 - T - 1, E);
-#pragma unroll
-    for (int i = 0; i < H; i++) {
-        const int k = k0 + i;
-        const C nw = rd<GUARD, ES>(s, k + T + 1, E);
-        const C od = rd<GUARD, ES>(s, k - T, E);
-        o[i] = c.out(acc, cadd(prev, nw));
-        acc = cadd(acc, nw);
-        acc = csub(acc, od);
-        prev = od;
-    }
-    acc = A1;
-    C od = rd<GUARD, ES>(s, k0 + K - 1 - T, E);
-#pragma unroll
-    for (int i = K - 1; i >= H; i--) {
-        const int k = k0 + i;
-        const C nw = rd<GUARD, ES>(s, k + T + 1, E);
-        acc = csub(acc, nw);
-        acc = cadd(acc, od);
-        const C tl = rd<GUARD, ES>(s, k - T - 1, E);
-        o[i] = c.out(acc, cadd(tl, nw));
-        od = tl;
-    }
-}
-
-// Narrow kernels (T <= DirectMax): every output is summed directly from the
-// K + 2T + 2 inputs the chunk needs, held in registers.  Sliding a window of
-// only a few cells over K/2 steps would carry the rounding error of large
-// values that have already left the window.
-template <typename C, int K, int ES, int TD, bool GUARD, bool SCALED>
-__device__ __forceinline__ void direct_pass(const C *__restrict__ s, int E, int k0, const PassCoef<C, SCALED> &c,
-                                            C (&o)[K])
-{
-    constexpr int NX = K + 2 * TD + 2;
-    C x[NX];
-#pragma unroll
-    for (int m = 0; m < NX; m++)
-        x[m] = rd<GUARD, ES>(s, k0 - TD - 1 + m, E);
-#pragma unroll
-    for (int i = 0; i < K; i++) {
-        C acc = x[i + 1];
-#pragma unroll
-        for (int d = 2; d <= 2 * TD + 1; d++)
-            acc = cadd(acc, x[i + d]);
-        o[i] = c.out(acc, cadd(x[i], x[i + 2 * TD + 2]));
-    }
-}
-
-template <typename Real>
-struct DirectMax;
-template <>
-struct DirectMax<float> {
-    static constexpr int T = 8;
-};
-template <>
-struct DirectMax<double> {
-    static constexpr int T = 3;
-};
-
-template <typename Real, typename C, int K, int ES, int TD, bool SCALED>
-__device__ __forceinline__ void direct_dispatch(int T, const C *s, int E, int k0, bool guard,
-                                                const PassCoef<C, SCALED> &c, C (&o)[K])
-{
-    if constexpr (TD <= DirectMax<Real>::T) {
-        if (T != TD) {
-            direct_dispatch<Real, C, K, ES, TD + 1, SCALED>(T, s, E, k0, guard, c, o);
-            return;
-        }
-        if (guard)
-            direct_pass<C, K, ES, TD, true, SCALED>(s, E, k0, c, o);
-        else
-            direct_pass<C, K, ES, TD, false, SCALED>(s, E, k0, c, o);
-    }
-}
-
-// Sums of a chunk that the next pass's anchors are built from: the whole
-// chunk (S), its first r2 cells (Pre) and its cells from r1 on (Suf).  Cells
-// at or beyond the line extent count as zero (tail chunk only).
-template <typename C, int K, bool TAIL>
-__device__ __forceinline__ void chunk_partials(const C (&o)[K], int k0, int E, int r1, int r2, C &S, C &Pre,
-                                               C &Suf)
-{
-    C s = czero<C>(), p = czero<C>(), u = czero<C>();
-#pragma unroll
-    for (int i = 0; i < K; i++) {
-        const C x = (!TAIL || k0 + i < E) ? o[i] : czero<C>();
-        s = cadd(s, x);
-        if (i < r2)
-            p = cadd(p, x);
-        if (i >= r1)
-            u = cadd(u, x);
-    }
-    S = s;
-    Pre = p;
-    Suf = u;
-}
-
-template <int PS, typename C>
-__device__ __forceinline__ C part_at(const C *__restrict__ a, int m, int nch)
-{
-    return (unsigned)m < (unsigned)nch ? a[m * PS] : czero<C>();
-}
-
-// Window sums at k0 = jK and k0 + K from the chunk partials (T >= 1):
-// window [k0-T, k0+T] = Suf[m1] + S[m1+1 .. m2-1] + Pre[m2], m1 = j - d1,
-// m2 = j + d2 (d1 = ceil(T/K), d2 = floor((T+1)/K)).  Every term is a sum of
-// cells inside the window: nothing is subtracted.
-template <int PS, typename C>
-__device__ __forceinline__ void anchors(const C *__restrict__ S, const C *__restrict__ Pre, const C *__restrict__ Suf,
-                                        int nch, int j, int d1, int d2, C &A0, C &A1)
-{
-    const int m1 = j - d1, m2 = j + d2;
-    C mid = czero<C>();
-    for (int m = m1 + 2; m <= m2 - 1; m++)
-        mid = cadd(mid, part_at<PS>(S, m, nch));
-    const bool two = (m2 - m1) >= 2;
-    A0 = cadd(cadd(cadd(part_at<PS>(Suf, m1, nch), two ? part_at<PS>(S, m1 + 1, nch) : czero<C>()), mid),
-              part_at<PS>(Pre, m2, nch));
-    A1 = cadd(cadd(cadd(part_at<PS>(Suf, m1 + 1, nch), mid), two ? part_at<PS>(S, m2, nch) : czero<C>()),
-              part_at<PS>(Pre, m2 + 1, nch));
-}
-
-// One box pass of one thread's chunk: outputs into o, next partials into S/P/U.
-template <typename Real, typename C, int K, int ES, int PS, bool SCALED>
-__device__ __forceinline__ void run_pass(const C *__restrict__ ln, const C *__restrict__ pp, int QS, int E, int nch,
-                                         int j, int T, int d1, int d2, int r1, int r2, bool direct,
-                                         const PassCoef<C, SCALED> &c, C (&o)[K], C &S, C &P, C &U)
-{
-    const int k0 = j * K;
-    const bool guard = (k0 - T - 1 < 0) || (k0 + K + T >= E);
-    if constexpr (K == K64) {
-        if (direct) {
-            direct_dispatch<Real, C, K, ES, 0, SCALED>(T, ln, E, k0, guard, c, o);
-            return;
-        }
-    }
-    C A0, A1;
-    anchors<PS>(pp, pp + QS, pp + 2 * QS, nch, j, d1, d2, A0, A1);
-    if (guard)
-        slide<C, K, ES, true, SCALED>(ln, E, k0, T, A0, A1, c, o);
-    else
-        slide<C, K, ES, false, SCALED>(ln, E, k0, T, A0, A1, c, o);
-    if (k0 + K <= E)
-        chunk_partials<C, K, false>(o, k0, E, r1, r2, S, P, U);
-    else
-        chunk_partials<C, K, true>(o, k0, E, r1, r2, S, P, U);
-}
-
-template <typename Real>
-__device__ __forceinline__ Real quotient(Real v, Real w, Real thr, double offset);
-template <>
-__device__ __forceinline__ double quotient<double>(double v, double w, double thr, double offset)
-{
-    // NaN where the weight is below the mask level, else vg / wg + offset
-    return (w < thr) ? __longlong_as_double(0x7ff8000000000000ll) : v / w + offset;
-}
-template <>
-__device__ __forceinline__ float quotient<float>(float v, float w, float thr, double offset)
-{
-    return (w < thr) ? __int_as_float(0x7fc00000) : v / w + (float)offset;
-}
-
-// ---------------------------------------------------------------------------
-// the splat (first axis, rows layout)
-// ---------------------------------------------------------------------------
-
-// One staged sample of one line: x position in cells, the line's row weights
-// (wy, wz of the reference's corner products) and the centred value.
-struct SplatRec {
-    double xc, wy, wz, v;
-};
-constexpr int kStage = 128;   // records staged per line per round
-
-// Sorted-sample ranges feeding one line (at most two, 3D).
-struct LineRanges {
-    uint32_t b[2], e[2];
-    int n;
-};
-
-template <int DIM>
-__device__ __forceinline__ LineRanges line_ranges(int64_t line, int64_t e0, int E, const Geometry &g,
-                                                  const SampleView &sv)
-{
-    LineRanges r;
-    r.n = 0;
-    if (DIM == 1) {
-        const int64_t lo = e0 >= 1 ? e0 - 1 : 0;
-        const int64_t hi = e0 + E - 1;
-        int64_t b0 = lo / sv.bin_w, b1 = hi / sv.bin_w;
-        if (b1 > (int64_t)sv.nbins - 1)
-            b1 = (int64_t)sv.nbins - 1;
-        if (b0 <= b1) {
-            r.b[0] = sv.bin_start[b0];
-            r.e[0] = sv.bin_start[b1 + 1];
-            r.n = 1;
-        }
-    } else if (DIM == 2) {
-        // samples whose lower corner row is line - 1 or line, in that order
-        const int64_t b0 = line >= 1 ? line - 1 : line;
-        r.b[0] = sv.bin_start[b0];
-        r.e[0] = sv.bin_start[line + 1];
-        r.n = 1;
-    } else {
-        const int64_t H = g.size[1];
-        const int64_t z = line / H, y = line % H;
-        for (int dz = 1; dz >= 0; dz--) {
-            if (z - dz < 0)
-                continue;
-            const int64_t rb = (z - dz) * H;
-            const int64_t b0 = y >= 1 ? rb + y - 1 : rb + y;
-            r.b[r.n] = sv.bin_start[b0];
-            r.e[r.n] = sv.bin_start[rb + y + 1];
-            r.n++;
-        }
-    }
-    return r;
-}
-
-// Position `pos` of the concatenated ranges -> sorted position.
-__device__ __forceinline__ uint32_t range_at(const LineRanges &r, uint32_t pos)
-{
-    const uint32_t n0 = r.n > 0 ? r.e[0] - r.b[0] : 0u;
-    return pos < n0 ? r.b[0] + pos : r.b[1] + (pos - n0);
-}
-
-__device__ __forceinline__ uint32_t range_total(const LineRanges &r)
-{
-    uint32_t t = 0;
-    for (int q = 0; q < r.n; q++)
-        t += r.e[q] - r.b[q];
-    return t;
-}
-
-template <int DIM>
-__device__ __forceinline__ SplatRec make_rec(uint32_t idx, int64_t line, const Geometry &g, const SampleView &sv,
-                                             double offset)
-{
-    SplatRec rc;
-    const double *p = sv.pts + (int64_t)idx * DIM;
-    rc.xc = (p[0] - g.x0[0]) / g.step[0];
-    rc.v = sv.val[idx] - offset;
-    rc.wy = 1.0;
-    rc.wz = 1.0;
-    if (DIM == 2) {
-        const double yc = (p[1] - g.x0[1]) / g.step[1];
-        const int64_t yi = (int64_t)yc;
-        const double yw = yc - (double)yi;
-        rc.wy = (yi == line) ? (1.0 - yw) : yw;
-    } else if (DIM == 3) {
-        const int64_t zl = line / g.size[1], yl = line % g.size[1];
-        const double yc = (p[1] - g.x0[1]) / g.step[1];
-        const int64_t yi = (int64_t)yc;
-        const double yw = yc - (double)yi;
-        rc.wy = (yi == yl) ? (1.0 - yw) : yw;
-        const double zc = (p[2] - g.x0[2]) / g.step[2];
-        const int64_t zi = (int64_t)zc;
-        const double zw = zc - (double)zi;
-        rc.wz = (zi == zl) ? (1.0 - zw) : zw;
-    }
-    return rc;
-}
-
-// Adds `cnt` staged records to one line, in order.  Lanes take 32 consecutive
-// records; lanes hitting the same cell add one after the other in lane order,
-// so the result does not depend on scheduling.
-template <typename Real, typename C, int DIM>
-__device__ void apply_recs(C *__restrict__ line, int E, int64_t e0, const SplatRec *__restrict__ rec, int cnt,
-                           int lane)
-{
-    const uint32_t lt = (1u << lane) - 1u;
-    for (int r = 0; r < cnt; r += 32) {
-        const bool valid = r + lane < cnt;
-        int64_t xi = 0;
-        double xw = 0.0, wy = 1.0, wz = 1.0, v = 0.0;
-        if (valid) {
-            const SplatRec rc = rec[r + lane];
-            xi = (int64_t)rc.xc;
-            xw = rc.xc - (double)xi;
-            wy = rc.wy;
-            wz = rc.wz;
-            v = rc.v;
-        }
-#pragma unroll
-        for (int c = 0; c < 2; c++) {
-            const int64_t ec = xi + c - e0;
-            const bool ok = valid && ec >= 0 && ec < E;
-            if (__ballot_sync(0xffffffffu, ok) == 0u)
-                continue;
-            // corner weight (wx * wy) * wz, the reference's product order
-            const double wx = c ? xw : (1.0 - xw);
-            double w = wx;
-            if (DIM >= 2)
-                w = wx * wy;
-            if (DIM == 3)
-                w = w * wz;
-            C add;
-            add.x = (Real)(w * v);
-            add.y = (Real)w;
-            const int key = ok ? (int)ec : -1 - lane;
-            const unsigned peers = __match_any_sync(0xffffffffu, key);
-            const int rank = __popc(peers & lt);
-            const int maxc = __reduce_max_sync(0xffffffffu, ok ? __popc(peers) : 0);
-            for (int q = 0; q < maxc; q++) {
-                if (ok && rank == q)
-                    line[ec] = cadd(line[ec], add);
-                __syncwarp();
-            }
-        }
-    }
-}
-
-// ---------------------------------------------------------------------------
-// the kernel
-// ---------------------------------------------------------------------------
-
-// Column-layout group width: 32 bytes of each grid row.
-template <typename C>
-struct ColG {
-    static constexpr int G = 32 / (int)sizeof(C);
-};
-
-// SPLAT_DIM: 0 = the lines are loaded from src, 1..3 = they are filled by
-// splatting the samples of a field of that dimension (rows layout).
-// LAYOUT: 0 = rows, 1 = columns.  K: chunk length (odd).
-template <typename Real, int K, int SPLAT_DIM, int LAYOUT>
-__global__ void __launch_bounds__(512, 1) k_axis(const AxisLaunch a, const Geometry g, const SampleView sv)
-{
-    using C = typename CellOf<Real>::T;
-    constexpr int G = LAYOUT == 0 ? 1 : ColG<C>::G;
-    constexpr int ES = G;   // cell stride inside a line buffer
-    constexpr int PS = G;   // chunk stride inside a partials array
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    C *cells = reinterpret_cast<C *>(smem_raw);
-    const int P = a.line_pitch;
-    const int CP = a.chunks_pad;
-    const int NLC = LAYOUT == 0 ? a.lines_per_cta : G;   // line slots in this CTA
-    C *part = cells + (size_t)NLC * P;                    // [3][NLC][CP] (rows) / [3][CP][G] (columns)
-    const int tid = threadIdx.x;
-    const int nthr = blockDim.x;
-
-    const int64_t group = blockIdx.x / a.ntiles;
-    const int64_t tile = blockIdx.x - group * a.ntiles;
-    const int64_t t0 = tile * a.tile_len;
-    const int64_t t1 = min(a.L, t0 + a.tile_len);
-    const int64_t e0 = max((int64_t)0, t0 - (int64_t)a.halo);
-    const int64_t e1 = min(a.L, t1 + (int64_t)a.halo);
-    const int E = (int)(e1 - e0);
-    const int nch = (E + K - 1) / K;
-
-    // lines of this CTA and their HBM position (cell e0 of the line)
-    int nl;                  // lines present
-    int64_t line0 = 0;       // rows: first line index
-    int64_t gbase = 0;       // columns: HBM cell index of (line 0 of the group, cell e0)
-    bool vec_ok = false;     // columns: the group's rows are whole aligned 32-byte segments
-    if (LAYOUT == 0) {
-        line0 = group * a.lines_per_cta;
-        nl = (int)min((int64_t)a.lines_per_cta, a.nlines - line0);
-    } else {
-        const int64_t o = group / a.xblocks, xb = group - o * a.xblocks;
-        nl = (int)min((int64_t)G, a.width - xb * G);
-        gbase = o * a.outer_stride + xb * G + e0 * a.elem_stride;
-        vec_ok = nl == G && (gbase % G) == 0 && (a.elem_stride % G) == 0;
-    }
-
-    // this thread's line / chunk
-    int li, j;
-    C *ln;
-    const C *pp0;
-    int QS;
-    if (LAYOUT == 0) {
-        li = tid / CP;
-        j = tid - li * CP;
-        ln = cells + (size_t)li * P;
-        QS = NLC * CP;
-        pp0 = part + (size_t)li * CP;
-    } else {
-        j = tid / G;
-        li = tid - j * G;
-        ln = cells + li;
-        QS = CP * G;
-        pp0 = part + li;
-    }
-    C *pw = const_cast<C *>(pp0) + (size_t)j * PS;   // this chunk's S slot
-    const bool active = li < nl && j < nch;
-    const int T = a.T;
-    const int d1 = (T + K - 1) / K, d2 = (T + 1) / K;
-    const int r1 = d1 * K - T, r2 = (T + 1) - d2 * K;
-    const double offset = (SPLAT_DIM != 0 || a.store_quot) ? field_offset(sv.hdr) : 0.0;
-
-    // ---- fill -------------------------------------------------------------
-    if constexpr (SPLAT_DIM != 0) {
-        // zero the line buffers, stage each line's samples with all of the
-        // line's threads, then the line's first warp adds them in order
-        float4 *z4 = reinterpret_cast<float4 *>(cells);
-        const int n4 = (int)((size_t)NLC * P * sizeof(C) / 16);
-        for (int i = tid; i < n4; i += nthr)
-            z4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        SplatRec *stage = reinterpret_cast<SplatRec *>(part + (size_t)3 * QS);
-        __shared__ uint32_t s_rounds;
-        if (tid == 0)
-            s_rounds = 0;
-        LineRanges rg;
-        rg.n = 0;
-        uint32_t total = 0;
-        if (li < nl) {
-            rg = line_ranges<SPLAT_DIM>(line0 + li, e0, E, g, sv);
-            total = range_total(rg);
-        }
-        __syncthreads();
-        if (li < nl && j == 0)
-            atomicMax(&s_rounds, (total + kStage - 1) / kStage);
-        __syncthreads();
-        const uint32_t rounds = s_rounds;
-        SplatRec *my_stage = stage + (size_t)li * kStage;
-        for (uint32_t rr = 0; rr < rounds; rr++) {
-            const uint32_t base = rr * kStage;
-            if (li < nl) {
-                for (int q = j; q < kStage; q += CP) {
-                    const uint32_t pos = base + q;
-                    if (pos < total)
-                        my_stage[q] = make_rec<SPLAT_DIM>(sv.sorted_idx[range_at(rg, pos)], line0 + li, g, sv,
-                                                          offset);
-                }
-            }
-            __syncthreads();
-            if (li < nl && j < 32 && base < total)
-                apply_recs<Real, C, SPLAT_DIM>(ln, E, e0, my_stage, (int)min((uint32_t)kStage, total - base), j);
-            __syncthreads();
-        }
-    } else if (LAYOUT == 0) {
-        if (a.plain) {
-            // single-field lines: the value half only
-            const Real *src = reinterpret_cast<const Real *>(a.src_v);
-            for (int q = 0; q < nl; q++) {
-                const Real *s_ = src + (line0 + q) * a.L + e0;
-                C *d_ = cells + (size_t)q * P;
-                for (int e = tid; e < E; e += nthr) {
-                    C c = czero<C>();
-                    c.x = s_[e];
-                    d_[e] = c;
-                }
-            }
-        } else {
-            const C *src = reinterpret_cast<const C *>(a.src_v);
-            for (int q = 0; q < nl; q++) {
-                const C *s_ = src + (line0 + q) * a.L + e0;
-                C *d_ = cells + (size_t)q * P;
-                for (int e = tid; e < E; e += nthr)
-                    d_[e] = s_[e];
-            }
-        }
-    } else {
-        const C *src = reinterpret_cast<const C *>(a.src_v) + gbase;
-        const int64_t es = a.elem_stride;
-        if (vec_ok) {
-            // two 16-byte vectors per row of G cells
-            const int nv = 2 * E;
-            uint4 *d_ = reinterpret_cast<uint4 *>(cells);
-#pragma unroll 4
-            for (int i = tid; i < nv; i += nthr) {
-                const int row = i >> 1, h = i & 1;
-                d_[i] = *reinterpret_cast<const uint4 *>(reinterpret_cast<const char *>(src + row * es) + 16 * h);
-            }
-        } else {
-            for (int i = tid; i < E * G; i += nthr) {
-                const int row = i / G, gg = i - row * G;
-                cells[i] = gg < nl ? src[row * es + gg] : czero<C>();
-            }
-        }
-    }
-    __syncthreads();
-
-    // ---- passes -----------------------------------------------------------
-    const bool direct = (K == K64) && T <= DirectMax<Real>::T;
-    if (active && !direct) {
-        // partials of the filled data
-        C o[K];
-        const int k0 = j * K;
-#pragma unroll
-        for (int i = 0; i < K; i++)
-            o[i] = (k0 + i < E) ? ln[(k0 + i) * ES] : czero<C>();
-        C S, Pr, Su;
-        chunk_partials<C, K, true>(o, k0, E, r1, r2, S, Pr, Su);
-        pw[0] = S;
-        pw[QS] = Pr;
-        pw[2 * QS] = Su;
-    }
-
-    PassCoef<C, false> cu;
-    cu.alpha = csplat<C>(a.alpha);
-    cu.inv = csplat<C>(1.0);
-    PassCoef<C, true> cs;
-    cs.alpha = csplat<C>(a.alpha * a.inv_norm);
-    cs.inv = csplat<C>(a.inv_norm);
-
-    for (int pass = 0; pass < a.passes; pass++) {
-        __syncthreads();
-        C o[K];
-        C S = czero<C>(), Pr = czero<C>(), Su = czero<C>();
-        if (active) {
-            if (a.scaled)
-                run_pass<Real, C, K, ES, PS, true>(ln, pp0, QS, E, nch, j, T, d1, d2, r1, r2, direct, cs, o, S, Pr,
-                                                   Su);
-            else
-                run_pass<Real, C, K, ES, PS, false>(ln, pp0, QS, E, nch, j, T, d1, d2, r1, r2, direct, cu, o, S, Pr,
-                                                    Su);
-        }
-        __syncthreads();
-        if (active) {
-            const int k0 = j * K;
-            if (k0 + K <= E) {
-#pragma unroll
-                for (int i = 0; i < K; i++)
-                    ln[(k0 + i) * ES] = o[i];
-            } else {
-#pragma unroll
-                for (int i = 0; i < K; i++)
-                    if (k0 + i < E)
-                        ln[(k0 + i) * ES] = o[i];
-            }
-            if (!direct) {
-                pw[0] = S;
-                pw[QS] = Pr;
-                pw[2 * QS] = Su;
-            }
-        }
-    }
-    __syncthreads();
-
-    // ---- store ------------------------------------------------------------
-    const int s0 = (int)(t0 - e0), s1 = (int)(t1 - e0);   // this tile's own cells
-    const Real thr = (Real)a.thr;
-    if (LAYOUT == 0) {
-        for (int q = 0; q < nl; q++) {
-            const C *c_ = cells + (size_t)q * P;
-            const int64_t gb = (line0 + q) * a.L + e0;
-            if (a.store_quot) {
-                if (a.out_f64) {
-                    double *o_ = reinterpret_cast<double *>(a.out) + gb;
-                    for (int e = s0 + tid; e < s1; e += nthr) {
-                        const C c = c_[e];
-                        o_[e] = (double)quotient<Real>(c.x, c.y, thr, offset);
-                    }
-                } else {
-                    float *o_ = reinterpret_cast<float *>(a.out) + gb;
-                    for (int e = s0 + tid; e < s1; e += nthr) {
-                        const C c = c_[e];
-                        o_[e] = (float)quotient<Real>(c.x, c.y, thr, offset);
-                    }
-                }
-            } else if (a.plain) {
-                Real *d_ = reinterpret_cast<Real *>(a.dst_v) + gb;
-                for (int e = s0 + tid; e < s1; e += nthr)
-                    d_[e] = c_[e].x;
-            } else {
-                C *d_ = reinterpret_cast<C *>(a.dst_v) + gb;
-                for (int e = s0 + tid; e < s1; e += nthr)
-                    d_[e] = c_[e];
-            }
-        }
-    } else {
-        const int64_t es = a.elem_stride;
-        if (a.store_quot) {
-            // one row of G cells per thread: G quotients, one vector store
-            const bool q_vec = G == 4 && vec_ok && (gbase % 4) == 0 && (es % 4) == 0;
-            for (int row = s0 + tid; row < s1; row += nthr) {
-                Real q[G];
-#pragma unroll
-                for (int u = 0; u < G; u++) {
-                    const C c = cells[row * G + u];
-                    q[u] = quotient<Real>(c.x, c.y, thr, offset);
-                }
-                const int64_t gi = gbase + row * es;
-                if (a.out_f64) {
-                    double *o_ = reinterpret_cast<double *>(a.out) + gi;
-#pragma unroll
-                    for (int u = 0; u < G; u++)
-                        if (u < nl)
-                            o_[u] = (double)q[u];
-                } else if (q_vec) {
-                    float4 v4;
-                    v4.x = (float)q[0];
-                    v4.y = (float)q[1 % G];
-                    v4.z = (float)q[2 % G];
-                    v4.w = (float)q[3 % G];
-                    *reinterpret_cast<float4 *>(reinterpret_cast<float *>(a.out) + gi) = v4;
-                } else {
-                    float *o_ = reinterpret_cast<float *>(a.out) + gi;
-#pragma unroll
-                    for (int u = 0; u < G; u++)
-                        if (u < nl)
-                            o_[u] = (float)q[u];
-                }
-            }
-        } else {
-            C *dst = reinterpret_cast<C *>(a.dst_v) + gbase;
-            if (vec_ok) {
-                const int nv = 2 * (s1 - s0);
-                const uint4 *s_ = reinterpret_cast<const uint4 *>(cells + (size_t)s0 * G);
-                for (int i = tid; i < nv; i += nthr) {
-                    const int row = s0 + (i >> 1), h = i & 1;
-                    *reinterpret_cast<uint4 *>(reinterpret_cast<char *>(dst + row * es) + 16 * h) = s_[i];
-                }
-            } else {
-                for (int i = tid; i < (s1 - s0) * G; i += nthr) {
-                    const int row = s0 + i / G, gg = i % G;
-                    if (gg < nl)
-                        dst[row * es + gg] = cells[row * G + gg];
-                }
-            }
-        }
-    }
-}
 
 // ---------------------------------------------------------------------------
 // host side
@@ -764,21 +15,26 @@ __global__ void __launch_bounds__(512, 1) k_axis(const AxisLaunch a, const Geome
 
 // Chunk length per launch.  Every output is at most K/2 sliding steps from an
 // exact anchor; in float32 that distance must stay short against the window
-// 2T+1, so windows up to 65 cells use the short chunk (and T <= 8 sums
-// directly), wider ones the long chunk with half the anchor overhead.
+// 2T+1.  The short chunk also keeps the kernels small enough for four CTAs
+// per SM; the long chunk (half the anchor overhead, more registers) can be
+// chosen with fb_tune("chunk", 33) for windows wider than 65 cells.
+static int g_chunk_choice = 0;   // 0 = automatic (short chunk), 17, 33
+
 static int chunk_k(int precision, int T)
 {
-    if (precision == 0)
+    if (precision == 0 || T <= 32)
         return K64;
-    return T <= 32 ? K64 : K32;
+    return g_chunk_choice == K32 ? K32 : K64;
 }
+
+static bool direct_mode(int precision, int T) { return T <= (precision == 0 ? DirectMax<double>::T : DirectMax<float>::T); }
 
 static int cell_size(int precision) { return precision == 0 ? 16 : 8; }
 static int col_g(int precision) { return 32 / cell_size(precision); }
 int axis_col_group(int precision) { return col_g(precision); }
 constexpr int kMaxThreads = 512;
 
-static size_t smem_limit()
+size_t axis_smem_limit()
 {
     static int lim = -1;
     if (lim < 0) {
@@ -800,11 +56,11 @@ size_t axis_smem_bytes(int precision, const AxisLaunch &a)
     const size_t nlc = a.layout == 0 ? (size_t)a.lines_per_cta : (size_t)col_g(precision);
     size_t b = nlc * ((size_t)a.line_pitch + 3 * (size_t)a.chunks_pad) * cs;
     if (a.fill_splat)
-        b += nlc * kStage * sizeof(SplatRec);
+        b += nlc * kStage * (precision == 0 ? sizeof(StageRec<double>) : sizeof(StageRec<float>));
     return b;
 }
 
-static int threads_of(int precision, const AxisLaunch &a)
+int axis_threads(int precision, const AxisLaunch &a)
 {
     if (a.layout == 0)
         return a.lines_per_cta * a.chunks_pad;
@@ -816,7 +72,7 @@ AxisPlanLimits axis_limits(int precision, int T)
     // the longest extent a rows-layout CTA (one line) and a columns-layout CTA
     // (G lines) can hold; the plan uses the one of its layout
     AxisPlanLimits l;
-    l.smem_limit = smem_limit();
+    l.smem_limit = axis_smem_limit();
     const int K = chunk_k(precision, T);
     int best[2] = {0, 0};
     for (int lay = 0; lay < 2; lay++) {
@@ -831,7 +87,7 @@ AxisPlanLimits axis_limits(int precision, int T)
             const int nch = (mid + K - 1) / K;
             const int unit = lay == 0 ? 32 : 32 / col_g(precision);
             a.chunks_pad = (nch + unit - 1) / unit * unit;
-            if (threads_of(precision, a) <= kMaxThreads && axis_smem_bytes(precision, a) <= l.smem_limit)
+            if (axis_threads(precision, a) <= kMaxThreads && axis_smem_bytes(precision, a) <= l.smem_limit)
                 lo = mid;
             else
                 hi = mid - 1;
@@ -856,7 +112,7 @@ bool axis_shape(int precision, AxisLaunch &a)
     a.line_pitch = pitch_of(E);
     if (a.layout == 1) {
         a.lines_per_cta = col_g(precision);
-        return threads_of(precision, a) <= kMaxThreads && axis_smem_bytes(precision, a) <= smem_limit();
+        return axis_threads(precision, a) <= kMaxThreads && axis_smem_bytes(precision, a) <= axis_smem_limit();
     }
     // rows: ~256 threads per CTA
     int nl = std::max(1, std::min<int>(std::max(1, 256 / a.chunks_pad), kMaxThreads / a.chunks_pad));
@@ -864,44 +120,16 @@ bool axis_shape(int precision, AxisLaunch &a)
         nl = (int)a.nlines;
     for (; nl >= 1; nl--) {
         a.lines_per_cta = nl;
-        if (axis_smem_bytes(precision, a) <= smem_limit() && threads_of(precision, a) <= kMaxThreads)
+        if (axis_smem_bytes(precision, a) <= axis_smem_limit() && axis_threads(precision, a) <= kMaxThreads)
             return true;
     }
     return false;
 }
 
-template <typename Real, int K, int SD, int LAY>
-static cudaError_t launch_one(const AxisLaunch &a, const Geometry &g, const SampleView &sv, cudaStream_t st)
-{
-    const int prec = sizeof(Real) == 8 ? 0 : 1;
-    const size_t smem = axis_smem_bytes(prec, a);
-    static bool configured = false;
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_axis<Real, K, SD, LAY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem_limit());
-        if (e != cudaSuccess)
-            return e;
-        configured = true;
-    }
-    const int64_t groups = a.layout == 0 ? (a.nlines + a.lines_per_cta - 1) / a.lines_per_cta
-                                         : a.outer_count * a.xblocks;
-    const int64_t blocks = groups * a.ntiles;
-    k_axis<Real, K, SD, LAY><<<(unsigned)blocks, threads_of(prec, a), smem, st>>>(a, g, sv);
-    return cudaGetLastError();
-}
-
-template <typename Real, int K>
-static cudaError_t launch_k(int sd, const AxisLaunch &a, const Geometry &g, const SampleView &sv, cudaStream_t st)
-{
-    if (a.layout == 1)
-        return launch_one<Real, K, 0, 1>(a, g, sv, st);
-    switch (sd) {
-    case 0: return launch_one<Real, K, 0, 0>(a, g, sv, st);
-    case 1: return launch_one<Real, K, 1, 0>(a, g, sv, st);
-    case 2: return launch_one<Real, K, 2, 0>(a, g, sv, st);
-    default: return launch_one<Real, K, 3, 0>(a, g, sv, st);
-    }
-}
+cudaError_t launch_axis_f32(int k, int mode, int sd, const AxisLaunch &a, const Geometry &g, const SampleView &sv,
+                            cudaStream_t st);
+cudaError_t launch_axis_f64(int mode, int sd, const AxisLaunch &a, const Geometry &g, const SampleView &sv,
+                            cudaStream_t st);
 
 cudaError_t launch_axis(int precision, const AxisLaunch &a, const Geometry &g, const SampleView &sv,
                         cudaStream_t st)
@@ -909,11 +137,19 @@ cudaError_t launch_axis(int precision, const AxisLaunch &a, const Geometry &g, c
     const int sd = a.fill_splat ? g.dim : 0;
     if (a.layout == 1 && a.fill_splat)
         return cudaErrorInvalidValue;
+    const int mode = direct_mode(precision, a.T) ? 1 : 0;
     if (precision == 0)
-        return launch_k<double, K64>(sd, a, g, sv, st);
-    if (chunk_k(precision, a.T) == K64)
-        return launch_k<float, K64>(sd, a, g, sv, st);
-    return launch_k<float, K32>(sd, a, g, sv, st);
+        return launch_axis_f64(mode, sd, a, g, sv, st);
+    return launch_axis_f32(mode == 1 ? K64 : chunk_k(precision, a.T), mode, sd, a, g, sv, st);
+}
+
+int axis_tune(const char *name, int value)
+{
+    if (strcmp(name, "chunk") == 0 && (value == 0 || value == K64 || value == K32)) {
+        g_chunk_choice = value;
+        return 0;
+    }
+    return -1;
 }
 
 cudaError_t launch_lines(int precision, void *data, int64_t nlines, int64_t len, int T, double alpha, int passes,

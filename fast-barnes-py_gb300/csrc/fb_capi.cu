@@ -38,6 +38,13 @@ static int cuda_fail(cudaError_t e, const char *where)
 extern "C" const char *fb_version(void) { return "fastbarnes_gb300 0.1 (sm_103a)"; }
 extern "C" const char *fb_last_error(void) { return g_err; }
 
+extern "C" int fb_tune(const char *name, int value)
+{
+    if (!name || axis_tune(name, value) != 0)
+        return fail(FB_ERR_ARG, "unknown tuning knob or value");
+    return FB_OK;
+}
+
 // ---------------------------------------------------------------------------
 // kernel-size helpers: fastbarnes/interpolation.py:543-569, :777-803
 // ---------------------------------------------------------------------------
@@ -278,7 +285,7 @@ int make_plan(int method, int precision, int dim, int64_t npts, const double *si
     p.off_bins = off;
     off = align_up(off + sizeof(uint32_t) * ((size_t)p.nbins + 1));
     p.off_sort = off;
-    off = align_up(off + sort_scratch_bytes(npts, p.nbins));
+    off = align_up(off + sort_scratch_bytes(npts, p.nbins, precision));
     for (int q = 0; q < p.pairs; q++) {
         p.off_pair[q] = off;
         off = align_up(off + 2 * sz * (size_t)p.npoints);
@@ -392,7 +399,9 @@ static int run_plan(Plan &p, const double *d_pts, const double *d_val, void *d_o
     uint32_t *bins = reinterpret_cast<uint32_t *>(ws + p.off_bins);
     uint32_t *scratch = reinterpret_cast<uint32_t *>(ws + p.off_sort);
     const uint32_t *sorted = nullptr;
-    cudaError_t e = sort_samples(d_pts, d_val, p.npts, p.g, p.bin_w, p.nbins, hdr, scratch, bins, &sorted, st);
+    const void *recs = nullptr;
+    cudaError_t e = sort_samples(p.precision, d_pts, d_val, p.npts, p.g, p.bin_w, p.nbins, hdr, scratch, bins,
+                                 &sorted, &recs, st);
     if (e != cudaSuccess)
         return cuda_fail(e, "sample sort");
     if (prof) {
@@ -401,8 +410,7 @@ static int run_plan(Plan &p, const double *d_pts, const double *d_val, void *d_o
         ev = e1;
     }
     SampleView sv{};
-    sv.pts = d_pts;
-    sv.val = d_val;
+    sv.rec = recs;
     sv.npts = p.npts;
     sv.sorted_idx = sorted;
     sv.bin_start = bins;

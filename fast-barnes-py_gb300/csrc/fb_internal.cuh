@@ -74,10 +74,29 @@ struct Geometry {
     double thr;           // NaN mask level on the unscaled weight field
 };
 
+// Cell coordinates of one sample, computed once by the bin-key kernel:
+// lower-corner cell (xi, yi, zi), fractional offsets inside it and the raw
+// value.  The float64 form keeps the reference's float64 offsets
+// xc - int(xc) (interpolation.py:251-254); the float32 form stores them as
+// float32.
+template <typename Real>
+struct SampleRec;
+template <>
+struct SampleRec<double> {
+    int32_t xi, yi, zi, pad;
+    double xw, yw, zw;
+    double val;
+};
+template <>
+struct SampleRec<float> {
+    int32_t xi, yi, zi;
+    float xw, yw, zw;
+    double val;
+};
+
 // Sorted-sample view handed to the splatting first-axis kernel.
 struct SampleView {
-    const double *pts;
-    const double *val;
+    const void *rec;              // SampleRec<Real>[npts], by sample index
     int64_t npts;
     const uint32_t *sorted_idx;   // sample indices ordered by bin (stable)
     const uint32_t *bin_start;    // nbins + 1 offsets into sorted_idx

@@ -5,10 +5,10 @@
 namespace fbg {
 
 // fb_sort.cu
-size_t sort_scratch_bytes(int64_t npts, uint32_t nbins);
-cudaError_t sort_samples(const double *pts, const double *val, int64_t npts, const Geometry &g,
-                         int bin_w, uint32_t nbins, FieldHeader *hdr, uint32_t *scratch,
-                         uint32_t *bin_start, const uint32_t **sorted_idx, cudaStream_t st);
+size_t sort_scratch_bytes(int64_t npts, uint32_t nbins, int precision);
+cudaError_t sort_samples(int precision, const double *pts, const double *val, int64_t npts, const Geometry &g,
+                         int bin_w, uint32_t nbins, FieldHeader *hdr, uint32_t *scratch, uint32_t *bin_start,
+                         const uint32_t **sorted_idx, const void **recs, cudaStream_t st);
 
 // fb_axis.cu
 struct AxisPlanLimits {
@@ -27,6 +27,8 @@ size_t axis_smem_bytes(int precision, const AxisLaunch &a);
 bool axis_shape(int precision, AxisLaunch &a);
 cudaError_t launch_axis(int precision, const AxisLaunch &a, const Geometry &g, const SampleView &sv,
                         cudaStream_t st);
+// Tuning knobs ("chunk": 0 automatic, 17 or 33); returns 0 if accepted.
+int axis_tune(const char *name, int value);
 // Standalone n-pass box filter over contiguous device lines (no splat, no
 // quotient): used for the reference's _accumulate_*_array entry points.
 cudaError_t launch_lines(int precision, void *data, int64_t nlines, int64_t len, int T, double alpha,

@@ -17,19 +17,23 @@
 
 namespace fbg {
 
-// Bin key of every sample (nbins for samples the reference skips), the count
-// of every bin, and the min / max / NaN reduction of the values.  The header
-// and the counts start zeroed (min is kept complemented for that reason).
-template <int DIM>
+// Bin key of every sample (nbins for samples the reference skips), its cell
+// record, the count of every bin, and the min / max / NaN reduction of the
+// values.  The header and the counts start zeroed (min is kept complemented
+// for that reason).  The float64 form divides by the step like the reference
+// (interpolation.py:247-248); the float32 form multiplies by its reciprocal.
+template <int DIM, typename Real>
 __global__ void k_bin_keys(const double *__restrict__ pts, const double *__restrict__ val, int64_t npts,
                            Geometry g, int bin_w, uint32_t nbins, uint32_t *__restrict__ keys,
-                           uint32_t *__restrict__ counts, FieldHeader *hdr)
+                           SampleRec<Real> *__restrict__ rec, uint32_t *__restrict__ counts, FieldHeader *hdr)
 {
+    constexpr bool EXACT = sizeof(Real) == 8;
+    const double inv0 = 1.0 / g.step[0], inv1 = 1.0 / g.step[1], inv2 = 1.0 / g.step[2];
     unsigned long long kmin = ~0ull, kmax = 0ull;
     int nan = 0;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < npts;
          k += (int64_t)gridDim.x * blockDim.x) {
-        double v = val[k];
+        const double v = val[k];
         if (isnan(v)) {
             nan = 1;
         } else {
@@ -39,21 +43,37 @@ __global__ void k_bin_keys(const double *__restrict__ pts, const double *__restr
         }
         uint32_t key = nbins;
         const double *p = pts + k * DIM;
-        double xc = (p[0] - g.x0[0]) / g.step[0];
-        if (DIM == 1) {
-            if (!(xc < 0.0 || xc >= (double)(g.size[0] - 1)))
-                key = (uint32_t)((int64_t)xc / bin_w);
-        } else if (DIM == 2) {
-            double yc = (p[1] - g.x0[1]) / g.step[1];
-            if (!(xc < 0.0 || yc < 0.0 || xc >= (double)(g.size[0] - 1) || yc >= (double)(g.size[1] - 1)))
-                key = (uint32_t)(int64_t)yc;
-        } else {
-            double yc = (p[1] - g.x0[1]) / g.step[1];
-            double zc = (p[2] - g.x0[2]) / g.step[2];
-            if (!(xc < 0.0 || yc < 0.0 || zc < 0.0 || xc >= (double)(g.size[0] - 1) ||
-                  yc >= (double)(g.size[1] - 1) || zc >= (double)(g.size[2] - 1)))
-                key = (uint32_t)((int64_t)zc * g.size[1] + (int64_t)yc);
+        const double xc = EXACT ? (p[0] - g.x0[0]) / g.step[0] : (p[0] - g.x0[0]) * inv0;
+        double yc = 0.0, zc = 0.0;
+        bool skip = xc < 0.0 || xc >= (double)(g.size[0] - 1);
+        if (DIM >= 2) {
+            yc = EXACT ? (p[1] - g.x0[1]) / g.step[1] : (p[1] - g.x0[1]) * inv1;
+            skip = skip || yc < 0.0 || yc >= (double)(g.size[1] - 1);
         }
+        if (DIM == 3) {
+            zc = EXACT ? (p[2] - g.x0[2]) / g.step[2] : (p[2] - g.x0[2]) * inv2;
+            skip = skip || zc < 0.0 || zc >= (double)(g.size[2] - 1);
+        }
+        SampleRec<Real> r;
+        r.xi = r.yi = r.zi = 0;
+        r.xw = r.yw = r.zw = 0;
+        if (!skip) {
+            const int64_t xi = (int64_t)xc, yi = (int64_t)yc, zi = (int64_t)zc;
+            r.xi = (int32_t)xi;
+            r.yi = (int32_t)yi;
+            r.zi = (int32_t)zi;
+            r.xw = (Real)(xc - (double)xi);
+            r.yw = (Real)(yc - (double)yi);
+            r.zw = (Real)(zc - (double)zi);
+            if (DIM == 1)
+                key = (uint32_t)(xi / bin_w);
+            else if (DIM == 2)
+                key = (uint32_t)yi;
+            else
+                key = (uint32_t)(zi * g.size[1] + yi);
+        }
+        r.val = v;
+        rec[k] = r;
         keys[k] = key;
         if (key < nbins)
             atomicAdd(&counts[key], 1u);
@@ -249,16 +269,18 @@ __global__ void __launch_bounds__(1024) k_sort_large(const uint32_t *__restrict_
     }
 }
 
-// Scratch layout (uint32): counts[nbins + 1] | cursor[nbins + 1] |
-// large[nbins + 2] | keys[N] | sorted[N] | big-bin scratch[2N].
-size_t sort_scratch_bytes(int64_t npts, uint32_t nbins)
+// Scratch layout: counts[nbins + 2] | cursor[nbins + 2] | large[nbins + 2] |
+// keys[N] | sorted[N] | big-bin scratch[2N] (uint32), then the sample records.
+size_t sort_scratch_bytes(int64_t npts, uint32_t nbins, int precision)
 {
-    return 4 * (3 * ((size_t)nbins + 2) + 4 * (size_t)npts) + 256;
+    const size_t words = 3 * ((size_t)nbins + 2) + 4 * (size_t)npts;
+    const size_t rec = precision == 0 ? sizeof(SampleRec<double>) : sizeof(SampleRec<float>);
+    return (4 * words + 255) / 256 * 256 + rec * (size_t)npts + 256;
 }
 
-cudaError_t sort_samples(const double *pts, const double *val, int64_t npts, const Geometry &g, int bin_w,
-                         uint32_t nbins, FieldHeader *hdr, uint32_t *scratch, uint32_t *bin_start,
-                         const uint32_t **sorted_idx, cudaStream_t st)
+cudaError_t sort_samples(int precision, const double *pts, const double *val, int64_t npts, const Geometry &g,
+                         int bin_w, uint32_t nbins, FieldHeader *hdr, uint32_t *scratch, uint32_t *bin_start,
+                         const uint32_t **sorted_idx, const void **recs, cudaStream_t st)
 {
     uint32_t *counts = scratch;
     uint32_t *cursor = counts + (nbins + 2);
@@ -266,20 +288,36 @@ cudaError_t sort_samples(const double *pts, const double *val, int64_t npts, con
     uint32_t *keys = large + (nbins + 2);
     uint32_t *sorted = keys + npts;
     uint32_t *big = sorted + npts;
+    const size_t words = 3 * ((size_t)nbins + 2) + 4 * (size_t)npts;
+    void *rec = reinterpret_cast<char *>(scratch) + (4 * words + 255) / 256 * 256;
     cudaError_t e = cudaMemsetAsync(hdr, 0, sizeof(FieldHeader), st);
     if (e == cudaSuccess)
         e = cudaMemsetAsync(counts, 0, sizeof(uint32_t) * 3 * ((size_t)nbins + 2), st);
     if (e != cudaSuccess)
         return e;
     *sorted_idx = sorted;
+    *recs = rec;
     if (npts > 0) {
         int blocks = (int)std::min<int64_t>((npts + 255) / 256, 152 * 8);
-        if (g.dim == 1)
-            k_bin_keys<1><<<blocks, 256, 0, st>>>(pts, val, npts, g, bin_w, nbins, keys, counts, hdr);
-        else if (g.dim == 2)
-            k_bin_keys<2><<<blocks, 256, 0, st>>>(pts, val, npts, g, bin_w, nbins, keys, counts, hdr);
-        else
-            k_bin_keys<3><<<blocks, 256, 0, st>>>(pts, val, npts, g, bin_w, nbins, keys, counts, hdr);
+#define FBG_KEYS(D, R)                                                                                            \
+    k_bin_keys<D, R><<<blocks, 256, 0, st>>>(pts, val, npts, g, bin_w, nbins, keys,                                \
+                                             reinterpret_cast<SampleRec<R> *>(rec), counts, hdr)
+        if (precision == 0) {
+            if (g.dim == 1)
+                FBG_KEYS(1, double);
+            else if (g.dim == 2)
+                FBG_KEYS(2, double);
+            else
+                FBG_KEYS(3, double);
+        } else {
+            if (g.dim == 1)
+                FBG_KEYS(1, float);
+            else if (g.dim == 2)
+                FBG_KEYS(2, float);
+            else
+                FBG_KEYS(3, float);
+        }
+#undef FBG_KEYS
     }
     k_scan_exclusive<<<1, 1024, 0, st>>>(counts, bin_start, (int64_t)nbins + 1);
     if (npts > 0) {

@@ -51,6 +51,11 @@ const char *fb_version(void);
 /* Message describing the last failure of the calling thread ("" if none). */
 const char *fb_last_error(void);
 
+/* Launch-shape knob, no reference counterpart: name "chunk" = cells per
+ * thread chunk of the float32 sliding passes for windows wider than 65 cells
+ * (0 = automatic, 17 or 33).  Used by the autotuner. */
+int fb_tune(const char *name, int value);
+
 /* ---- kernel-size helpers (host only) --------------------------------------
  * Replace fastbarnes/interpolation.py:543-569 (get_half_kernel_size_opt,
  * get_tail_value) and :777-803 (get_half_kernel_size, get_sigma_effective). */
