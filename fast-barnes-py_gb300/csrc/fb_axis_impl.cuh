@@ -9,7 +9,8 @@
 //
 // The value and the weight field travel together as one cell (v, w): a float2
 // in the float32 form, whose two halves every pass updates with one packed
-// instruction (add/fma .f32x2), or a double2 in the float64 form.  Cells are
+// instruction (add / fma .f32x2 via __fadd2_rn / __ffma2_rn), or a double2 in
+// the float64 form.  Cells are
 // interleaved the same way in HBM between axes.
 //
 // One CTA holds whole lines (or halo-extended tiles of long lines) in shared
@@ -58,43 +59,11 @@ struct CellOf<double> {
     using T = double2;
 };
 
-__device__ __forceinline__ unsigned long long pk(float2 a)
-{
-    unsigned long long r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
-    return r;
-}
-__device__ __forceinline__ float2 upk(unsigned long long r)
-{
-    float2 a;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
-    return a;
-}
-
-__device__ __forceinline__ float2 cadd(float2 a, float2 b)
-{
-    unsigned long long d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)));
-    return upk(d);
-}
-__device__ __forceinline__ float2 csub(float2 a, float2 b)
-{
-    unsigned long long d;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)));
-    return upk(d);
-}
-__device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c)
-{
-    unsigned long long d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)), "l"(pk(c)));
-    return upk(d);
-}
-__device__ __forceinline__ float2 cmul(float2 a, float2 b)
-{
-    unsigned long long d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)));
-    return upk(d);
-}
+// float32 pairs: the packed .f32x2 instructions through CUDA's intrinsics
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ double2 cfma(double2 a, double2 b, double2 c)
@@ -462,11 +431,9 @@ struct ColG {
 // SPLAT_DIM: 0 = the lines are loaded from src, 1..3 = they are filled by
 // splatting the samples of a field of that dimension (rows layout).
 // LAYOUT: 0 = rows, 1 = columns.  K: chunk length (odd).
-// MODE: 0 = sliding windows, 1 = direct sums (narrow kernels).  The sliding
-// short-chunk kernels are held to 64 registers so that four CTAs of 256
-// threads share an SM.
+// MODE: 0 = sliding windows, 1 = direct sums (narrow kernels).
 template <typename Real, int K, int MODE, int SPLAT_DIM, int LAYOUT>
-__global__ void __launch_bounds__(512, (MODE == 0 && K == K64 && sizeof(Real) == 4) ? 2 : 1)
+__global__ void __launch_bounds__(512, 1)
     k_axis(const AxisLaunch a, const Geometry g, const SampleView sv)
 {
     using C = typename CellOf<Real>::T;
