@@ -15,16 +15,16 @@ namespace fbg {
 
 // Chunk length per launch.  Every output is at most K/2 sliding steps from an
 // exact anchor; in float32 that distance must stay short against the window
-// 2T+1.  The short chunk also keeps the kernels small enough for four CTAs
-// per SM; the long chunk (half the anchor overhead, more registers) can be
-// chosen with fb_tune("chunk", 33) for windows wider than 65 cells.
-static int g_chunk_choice = 0;   // 0 = automatic (short chunk), 17, 33
+// 2T+1, so windows up to 65 cells use the short chunk; wider windows use the
+// long chunk (half the anchor overhead) unless fb_tune("chunk", 17) asks for
+// the short one.
+static int g_chunk_choice = 0;   // 0 = automatic, 17, 33
 
 static int chunk_k(int precision, int T)
 {
     if (precision == 0 || T <= 32)
         return K64;
-    return g_chunk_choice == K32 ? K32 : K64;
+    return g_chunk_choice == K64 ? K64 : K32;
 }
 
 static bool direct_mode(int precision, int T) { return T <= (precision == 0 ? DirectMax<double>::T : DirectMax<float>::T); }

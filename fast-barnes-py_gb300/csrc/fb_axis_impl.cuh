@@ -432,15 +432,15 @@ struct ColG {
 // splatting the samples of a field of that dimension (rows layout).
 // LAYOUT: 0 = rows, 1 = columns.  K: chunk length (odd).
 // MODE: 0 = sliding windows, 1 = direct sums (narrow kernels).
+// One tile of one launch: line group `group`, tile `tile` along the lines.
 template <typename Real, int K, int MODE, int SPLAT_DIM, int LAYOUT>
-__global__ void __launch_bounds__(512, 1)
-    k_axis(const AxisLaunch a, const Geometry g, const SampleView sv)
+__device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g, const SampleView &sv, int64_t group,
+                                          int64_t tile, unsigned char *smem_raw)
 {
     using C = typename CellOf<Real>::T;
     constexpr int G = LAYOUT == 0 ? 1 : ColG<C>::G;
     constexpr int ES = G;   // cell stride inside a line buffer
     constexpr int PS = G;   // chunk stride inside a partials array
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     C *cells = reinterpret_cast<C *>(smem_raw);
     const int P = a.line_pitch;
     const int CP = a.chunks_pad;
@@ -449,8 +449,6 @@ __global__ void __launch_bounds__(512, 1)
     const int tid = threadIdx.x;
     const int nthr = blockDim.x;
 
-    const int64_t group = blockIdx.x / a.ntiles;
-    const int64_t tile = blockIdx.x - group * a.ntiles;
     const int64_t t0 = tile * a.tile_len;
     const int64_t t1 = min(a.L, t0 + a.tile_len);
     const int64_t e0 = max((int64_t)0, t0 - (int64_t)a.halo);
@@ -722,6 +720,51 @@ __global__ void __launch_bounds__(512, 1)
                 }
             }
         }
+    }
+}
+
+template <typename Real, int K, int MODE, int SPLAT_DIM, int LAYOUT>
+__global__ void __launch_bounds__(512, 1) k_axis(const AxisLaunch a, const Geometry g, const SampleView sv)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int64_t group = blockIdx.x / a.ntiles;
+    axis_tile<Real, K, MODE, SPLAT_DIM, LAYOUT>(a, g, sv, group, blockIdx.x - group * a.ntiles, smem_raw);
+}
+
+// Batched form: the CTAs of one launch take work items (field, block of that
+// field's launch) from a counter until none is left, largest fields first, so
+// fields of uneven size share the GPU without a tail per field.  No CTA waits
+// for another: each item is independent.
+struct BatchAxisField {
+    AxisLaunch a;
+    Geometry g;
+    SampleView sv;
+};
+struct BatchItem {
+    uint32_t field;
+    uint32_t block;
+};
+
+template <typename Real, int K, int MODE, int SPLAT_DIM, int LAYOUT>
+__global__ void __launch_bounds__(512, 1) k_axis_batch(const BatchAxisField *__restrict__ fields,
+                                                       const BatchItem *__restrict__ items, uint32_t nitems,
+                                                       uint32_t *__restrict__ counter)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ uint32_t s_item;
+    for (;;) {
+        if (threadIdx.x == 0)
+            s_item = atomicAdd(counter, 1u);
+        __syncthreads();
+        const uint32_t it = s_item;
+        __syncthreads();
+        if (it >= nitems)
+            break;
+        const BatchItem bi = items[it];
+        const BatchAxisField &f = fields[bi.field];
+        const int64_t group = bi.block / f.a.ntiles;
+        axis_tile<Real, K, MODE, SPLAT_DIM, LAYOUT>(f.a, f.g, f.sv, group, bi.block - group * f.a.ntiles, smem_raw);
+        __syncthreads();
     }
 }
 

@@ -94,6 +94,19 @@ struct SampleRec<float> {
     double val;
 };
 
+// One 2D field of a batch, as the batched bin-key kernel sees it.
+struct BatchKeyField {
+    const double *pts;
+    const double *val;
+    int64_t npts;
+    int64_t sample_offset;   // first global sample index of the field
+    uint32_t bin_offset;     // first global bin (row) of the field
+    uint32_t pad;
+    double x0[2], step[2];
+    int64_t size[2];
+};
+constexpr int kBatchKeysPerBlock = 2048;
+
 // Sorted-sample view handed to the splatting first-axis kernel.
 struct SampleView {
     const void *rec;              // SampleRec<Real>[npts], by sample index

@@ -10,6 +10,11 @@ cudaError_t sort_samples(int precision, const double *pts, const double *val, in
                          int bin_w, uint32_t nbins, FieldHeader *hdr, uint32_t *scratch, uint32_t *bin_start,
                          const uint32_t **sorted_idx, const void **recs, cudaStream_t st);
 
+size_t batch_sort_scratch_bytes(int64_t ntot, uint32_t nbins, int precision);
+cudaError_t batch_sort(int precision, const BatchKeyField *d_fields, const uint2 *d_blocks, uint32_t nblocks,
+                       int64_t ntot, uint32_t nbins, FieldHeader *hdrs, int nfields, uint32_t *scratch,
+                       uint32_t *bin_start, const uint32_t **sorted_idx, const void **recs, cudaStream_t st);
+
 // fb_axis.cu
 struct AxisPlanLimits {
     int extent_max;        // longest line extent a rows-layout CTA holds

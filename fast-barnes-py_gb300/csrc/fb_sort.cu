@@ -269,6 +269,198 @@ __global__ void __launch_bounds__(1024) k_sort_large(const uint32_t *__restrict_
     }
 }
 
+// ---------------------------------------------------------------------------
+// batched form: the samples of many 2D fields in one set of launches
+// ---------------------------------------------------------------------------
+
+// Bin keys and records of one block of one field's samples; keys are global
+// bins (the field's bin offset + row), records indexed by global sample.
+template <typename Real>
+__global__ void k_batch_keys(const BatchKeyField *__restrict__ fields, const uint2 *__restrict__ blocks,
+                             uint32_t skip_key, uint32_t *__restrict__ keys, SampleRec<Real> *__restrict__ rec,
+                             uint32_t *__restrict__ counts, FieldHeader *__restrict__ hdrs)
+{
+    constexpr bool EXACT = sizeof(Real) == 8;
+    const uint2 bt = blocks[blockIdx.x];   // (field, first sample of the block within the field)
+    const BatchKeyField f = fields[bt.x];
+    const double inv0 = 1.0 / f.step[0], inv1 = 1.0 / f.step[1];
+    unsigned long long kmin = ~0ull, kmax = 0ull;
+    int nan = 0;
+    const int64_t end = min(f.npts, (int64_t)bt.y + kBatchKeysPerBlock);
+    for (int64_t k = (int64_t)bt.y + threadIdx.x; k < end; k += blockDim.x) {
+        const double v = f.val[k];
+        if (isnan(v)) {
+            nan = 1;
+        } else {
+            unsigned long long o = dbl_to_ordered(v);
+            kmin = o < kmin ? o : kmin;
+            kmax = o > kmax ? o : kmax;
+        }
+        const double *p = f.pts + 2 * k;
+        const double xc = EXACT ? (p[0] - f.x0[0]) / f.step[0] : (p[0] - f.x0[0]) * inv0;
+        const double yc = EXACT ? (p[1] - f.x0[1]) / f.step[1] : (p[1] - f.x0[1]) * inv1;
+        const bool skip = xc < 0.0 || yc < 0.0 || xc >= (double)(f.size[0] - 1) || yc >= (double)(f.size[1] - 1);
+        SampleRec<Real> r;
+        r.xi = r.yi = r.zi = 0;
+        r.xw = r.yw = r.zw = 0;
+        uint32_t key = skip_key;
+        if (!skip) {
+            const int64_t xi = (int64_t)xc, yi = (int64_t)yc;
+            r.xi = (int32_t)xi;
+            r.yi = (int32_t)yi;
+            r.xw = (Real)(xc - (double)xi);
+            r.yw = (Real)(yc - (double)yi);
+            key = f.bin_offset + (uint32_t)yi;
+        }
+        r.val = v;
+        const int64_t gk = f.sample_offset + k;
+        rec[gk] = r;
+        keys[gk] = key;
+        if (key < skip_key)
+            atomicAdd(&counts[key], 1u);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long a = __shfl_xor_sync(0xffffffffu, kmin, o);
+        unsigned long long b = __shfl_xor_sync(0xffffffffu, kmax, o);
+        kmin = a < kmin ? a : kmin;
+        kmax = b > kmax ? b : kmax;
+    }
+    nan = __any_sync(0xffffffffu, nan);
+    if ((threadIdx.x & 31) == 0) {
+        FieldHeader *hdr = hdrs + bt.x;
+        if (kmin != ~0ull)
+            atomicMax(&hdr->vmin_key, ~kmin);
+        if (kmax != 0ull)
+            atomicMax(&hdr->vmax_key, kmax);
+        if (nan)
+            atomicExch(&hdr->nan_seen, 1);
+    }
+}
+
+// Device-wide exclusive scan in three steps: sums of 4096-entry tiles, an
+// exclusive scan of the tile sums (one block), and every tile scanned from
+// its offset.
+__global__ void __launch_bounds__(1024) k_tile_sums(const uint32_t *__restrict__ in, int64_t n,
+                                                    uint32_t *__restrict__ sums)
+{
+    __shared__ uint32_t ws[32];
+    const int64_t base = (int64_t)blockIdx.x * 4096;
+    uint32_t s = 0;
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+        const int64_t i = base + 4 * threadIdx.x + u;
+        s += i < n ? in[i] : 0u;
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0)
+        ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        uint32_t t = ws[threadIdx.x];
+        for (int o = 16; o > 0; o >>= 1)
+            t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (threadIdx.x == 0)
+            sums[blockIdx.x] = t;
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_tile_scan(const uint32_t *__restrict__ in, int64_t n,
+                                                    const uint32_t *__restrict__ offs, uint32_t *__restrict__ out)
+{
+    __shared__ uint32_t wsum[32];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const int64_t base = (int64_t)blockIdx.x * 4096;
+    uint32_t x[4], s = 0;
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+        const int64_t i = base + 4 * t + u;
+        x[u] = i < n ? in[i] : 0u;
+        s += x[u];
+    }
+    uint32_t inc = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o)
+            inc += y;
+    }
+    if (lane == 31)
+        wsum[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        const uint32_t v = wsum[lane];
+        uint32_t wi = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o)
+                wi += y;
+        }
+        wsum[lane] = wi - v;
+    }
+    __syncthreads();
+    uint32_t run = offs[blockIdx.x] + wsum[w] + inc - s;
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+        const int64_t i = base + 4 * t + u;
+        if (i < n)
+            out[i] = run;
+        run += x[u];
+    }
+}
+
+size_t batch_sort_scratch_bytes(int64_t ntot, uint32_t nbins, int precision)
+{
+    const size_t tiles = ((size_t)nbins + 1 + 4095) / 4096;
+    return sort_scratch_bytes(ntot, nbins, precision) + 8 * tiles + 256;
+}
+
+cudaError_t batch_sort(int precision, const BatchKeyField *d_fields, const uint2 *d_blocks, uint32_t nblocks,
+                       int64_t ntot, uint32_t nbins, FieldHeader *hdrs, int nfields, uint32_t *scratch,
+                       uint32_t *bin_start, const uint32_t **sorted_idx, const void **recs, cudaStream_t st)
+{
+    uint32_t *counts = scratch;
+    uint32_t *cursor = counts + (nbins + 2);
+    uint32_t *large = cursor + (nbins + 2);
+    uint32_t *keys = large + (nbins + 2);
+    uint32_t *sorted = keys + ntot;
+    uint32_t *big = sorted + ntot;
+    const size_t words = 3 * ((size_t)nbins + 2) + 4 * (size_t)ntot;
+    char *rec = reinterpret_cast<char *>(scratch) + (4 * words + 255) / 256 * 256;
+    const size_t recb = precision == 0 ? sizeof(SampleRec<double>) : sizeof(SampleRec<float>);
+    uint32_t *tsum = reinterpret_cast<uint32_t *>(rec + ((recb * (size_t)ntot + 255) / 256 * 256));
+    cudaError_t e = cudaMemsetAsync(hdrs, 0, sizeof(FieldHeader) * (size_t)nfields, st);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(counts, 0, sizeof(uint32_t) * 3 * ((size_t)nbins + 2), st);
+    if (e != cudaSuccess)
+        return e;
+    *sorted_idx = sorted;
+    *recs = rec;
+    if (nblocks > 0) {
+        if (precision == 0)
+            k_batch_keys<double><<<nblocks, 256, 0, st>>>(d_fields, d_blocks, nbins, keys,
+                                                           reinterpret_cast<SampleRec<double> *>(rec), counts, hdrs);
+        else
+            k_batch_keys<float><<<nblocks, 256, 0, st>>>(d_fields, d_blocks, nbins, keys,
+                                                          reinterpret_cast<SampleRec<float> *>(rec), counts, hdrs);
+    }
+    const int64_t n = (int64_t)nbins + 1;
+    const unsigned tiles = (unsigned)((n + 4095) / 4096);
+    k_tile_sums<<<tiles, 1024, 0, st>>>(counts, n, tsum);
+    uint32_t *toff = tsum + tiles;
+    k_scan_exclusive<<<1, 1024, 0, st>>>(tsum, toff, (int64_t)tiles);
+    k_tile_scan<<<tiles, 1024, 0, st>>>(counts, n, toff, bin_start);
+    if (ntot > 0) {
+        int blocks = (int)std::min<int64_t>((ntot + 255) / 256, 152 * 8);
+        k_bin_scatter<<<blocks, 256, 0, st>>>(keys, ntot, nbins, bin_start, cursor, sorted);
+        k_sort_bins<<<(unsigned)((nbins + kBinSortWarps - 1) / kBinSortWarps), 32 * kBinSortWarps, 0, st>>>(
+            bin_start, nbins, sorted, large);
+        k_sort_large<<<64, 1024, 0, st>>>(bin_start, sorted, large, big);
+    }
+    return cudaGetLastError();
+}
+
 // Scratch layout: counts[nbins + 2] | cursor[nbins + 2] | large[nbins + 2] |
 // keys[N] | sorted[N] | big-bin scratch[2N] (uint32), then the sample records.
 size_t sort_scratch_bytes(int64_t npts, uint32_t nbins, int precision)
