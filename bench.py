@@ -7,15 +7,18 @@ values 1000 + 20 sin(lon/10) cos(lat/8) + N(0, 2^2), sigma = 1 degree,
 num_iter = 4, max_dist = 3.5; float32-compensated form (fp32c).  Seeded
 synthetic data stand in for observations.
 
-Metric: Mgridpts/s = batch grid points x steps / time.  `value` runs the
-device entry point with inputs resident in HBM; `e2e` runs the C-ABI host
-entry (fb_interpolate_host) from pinned host buffers, copies included.  The
-plain float64 form of the same batch, its error against the float64 result
-and the CPU oracle (the reference's algorithm restated in C) are reported
-beside it.
+Metric: Mgridpts/s = batch grid points x steps / time.  One step is one run
+of a batch plan (fb_batch_run: one sample sort and one persistent launch per
+axis for all B fields, replayed from a CUDA graph).  `value` has the inputs
+resident in HBM; `e2e` runs the C-ABI host-buffer form (fb_batch_run_host)
+from pinned host buffers, copies of every field's samples in and results out
+included.  The plain float64 form of the same batch, its error against the
+float64 result, the one-call-per-field entry (fb_interpolate) and the CPU
+oracle (the reference's algorithm restated in C) are reported beside it.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--batch B]
                        [--precision fp32c|fp64] [--impl gpu|reference]
+                       [--knobs CHUNK,ROWS] [--quick]
 For N > 1 (torchrun) every rank runs its own batch (replicas: the fields are
 independent, no collective on the data path); rank 0 prints the JSON line.
 """
@@ -188,7 +191,7 @@ def main():
     ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--chunk", type=int, default=0, help="fb_tune chunk knob (0 automatic, 17, 33)")
+    ap.add_argument("--knobs", default="", help="pin the launch shape 'chunk,rows_threads' instead of tuning")
     ap.add_argument("--quick", action="store_true",
                     help="warm-up and timed steps only (no fp64 form, e2e or CPU baseline): for profiler runs")
     args = ap.parse_args()
@@ -201,6 +204,7 @@ def main():
 
     import torch
     from fastbarnes_gb300 import _lib
+    from fastbarnes_gb300.batched import BatchPlan
     if world > 1:
         import torch.distributed as dist
         torch.cuda.set_device(local)
@@ -209,136 +213,165 @@ def main():
         torch.cuda.set_device(0)
     dev = torch.device("cuda", torch.cuda.current_device())
     L = _lib.lib()
-    _lib.check(L.fb_tune(b"chunk", args.chunk), "fb_tune")
     prec = _lib.PRECISIONS[args.precision]
     B = args.batch
+    knobs = tuple(int(x) for x in args.knobs.split(",")) if args.knobs else None
 
     # device-resident inputs, one output per field
-    fields = [field_inputs(1000 + 97 * rank + f) for f in range(B)]
-    d_pts = [torch.as_tensor(p, device=dev) for p, _ in fields]
-    d_val = [torch.as_tensor(v, device=dev) for _, v in fields]
-    outs = [torch.empty((H, W), dtype=torch.float32, device=dev) for _ in range(B)]
-    d = _lib.dvec
-    c_sigma, c_x0, c_step = d([SIGMA, SIGMA]), d(list(X0)), d(list(STEP))
-    c_size = d([W, H], ctypes.c_int64)
-    mdw = math.exp(-MAX_DIST ** 2 / 2)
-    need = ctypes.c_size_t(0)
-
-    def ws_for(pc):
-        _lib.check(L.fb_workspace_size(0, pc, 2, NPTS, c_sigma, c_step, c_size, NITER, ctypes.byref(need)))
-        return torch.empty(need.value, dtype=torch.uint8, device=dev)
-
-    ws = ws_for(prec)
+    host = [field_inputs(1000 + 97 * rank + f) for f in range(B)]
+    fields = [dict(pts=torch.as_tensor(p, device=dev), val=torch.as_tensor(v, device=dev), sigma=SIGMA, x0=X0,
+                   step=STEP, size=(W, H), num_iter=NITER, max_dist=MAX_DIST) for p, v in host]
+    plan = BatchPlan(fields, precision=args.precision, graph=True, tune=knobs is None, knobs=knobs, device=dev)
+    knobs = plan.knobs
+    launches_per_step, memsets_per_step, plan_bytes = plan.info
     stream = torch.cuda.current_stream(dev)
-    sptr = ctypes.c_void_p(stream.cuda_stream)
-
-    def step(pc=prec, wsb=ws, out_list=outs, out_f64=0):
-        for f in range(B):
-            rc = L.fb_interpolate(0, pc, 2, d_pts[f].data_ptr(), d_val[f].data_ptr(), NPTS, c_sigma, c_x0, c_step,
-                                  c_size, NITER, mdw, out_list[f].data_ptr(), out_f64, wsb.data_ptr(), wsb.numel(),
-                                  sptr)
-            if rc != 0:
-                _lib.check(rc, "fb_interpolate")
 
     for _ in range(args.warmup):
-        step()
+        plan.run(stream)
     torch.cuda.synchronize()
 
-    # ---- timed region: device entry, inputs resident in HBM --------------
-    _lib.check(L.fb_profile_begin())
+    # ---- timed region: batch plan replayed from its CUDA graph, inputs in HBM
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
         barrier(world)
         torch.cuda.synchronize()
         ev0.record(stream)
         for _ in range(args.steps):
-            step()
+            plan.run(stream)
         ev1.record(stream)
         torch.cuda.synchronize()
         barrier(world)
     t_ms = ev0.elapsed_time(ev1)
-    maxrec = 64 * args.steps * B
-    stages = (ctypes.c_int * maxrec)()
-    times = (ctypes.c_float * maxrec)()
-    nrec = ctypes.c_int(0)
-    _lib.check(L.fb_profile_end(stages, times, maxrec, ctypes.byref(nrec)))
     t_ms = max_over_ranks(world, t_ms)
     gridpts = W * H * B * args.steps * world
     value = gridpts / (t_ms / 1e3) / 1e6
 
-    # per-stage launch times -> roofline of the dominant kernel
+    # ---- per-stage launch times (same plan shape, launched without the graph
+    # so that events can sit between its launches) -> roofline
+    prof_plan = BatchPlan(fields, precision=args.precision, graph=False, knobs=knobs, device=dev)
+    for _ in range(2):
+        prof_plan.run(stream)
+    torch.cuda.synchronize()
+    nprof = max(3, min(args.steps, 10))
+    _lib.check(L.fb_profile_begin())
+    for _ in range(nprof):
+        prof_plan.run(stream)
+    maxrec = 8 * nprof
+    stages = (ctypes.c_int * maxrec)()
+    times = (ctypes.c_float * maxrec)()
+    nrec = ctypes.c_int(0)
+    _lib.check(L.fb_profile_end(stages, times, maxrec, ctypes.byref(nrec)))
+    prof_plan.close()
     per_stage = {}
     for i in range(nrec.value):
         per_stage.setdefault(stages[i], []).append(times[i])
     sz = 4 if prec == _lib.FB_FP32C else 8
-    alg = {0: NPTS * (24 + 4 * 6),                           # sort: coords+value read, keys / indices
-           1: NPTS * 28 + W * H * 2 * sz,                    # splat + row passes: samples in, v,w out
-           2: W * H * 2 * sz + W * H * 4}                    # column passes + quotient: v,w in, float32 out
-    names = {0: "sample sort", 1: "k_axis x-passes (splat fused)", 2: "k_axis y-passes (quotient fused)"}
-    stage_ms = {k: sum(v) / len(v) for k, v in per_stage.items()}
-    dom = max((k for k in stage_ms if k != 0), key=lambda k: sum(per_stage[k]))
+    # algorithmic HBM bytes of one launch (all B fields): the sort reads the
+    # samples (16 + 8 B) and writes / reads keys, indices and records; the
+    # x launch reads the sample records (28 B) and writes the (v, w) field;
+    # the y launch reads it and writes the float32 result
+    alg = {0: B * NPTS * (24 + 4 * 6),
+           1: B * (NPTS * 28 + W * H * 2 * sz),
+           2: B * (W * H * 2 * sz + W * H * 4)}
+    names = {0: "sample sort (7 kernels)", 1: "k_axis_batch x (splat fused)", 2: "k_axis_batch y (quotient fused)"}
+    stage_ms = {k: statistics.median(v) for k, v in per_stage.items()}
+    dom = max((k for k in stage_ms if k != 0), key=lambda k: stage_ms[k])
     peak, peak_kind = measured_peak()
     achieved = alg[dom] / (stage_ms[dom] / 1e3) / 1e9
-    pipeline_bytes = NPTS * 28 + W * H * (4 * sz + 4)
-    pipeline_gbs = pipeline_bytes * B * args.steps / (t_ms / 1e3) / 1e9
+    pipeline_bytes = B * (NPTS * 28 + W * H * (4 * sz + 4))
+    pipeline_gbs = pipeline_bytes * args.steps / (t_ms / 1e3) / 1e9
 
     if args.quick:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": "Mgridpts/s", "quick": True,
+                              "knobs": knobs, "ms_per_step": t_ms / args.steps,
                               "stage_ms": {names[k]: v for k, v in stage_ms.items()}}), flush=True)
+        plan.close()
         return
 
     # ---- plain float64 form of the same batch + error at fixed config -----
-    ws64 = ws_for(_lib.FB_FP64) if prec != _lib.FB_FP64 else ws
-    outs64 = [torch.empty((H, W), dtype=torch.float64, device=dev) for _ in range(B)]
-    step(_lib.FB_FP64, ws64, outs64, 1)
+    plan64 = BatchPlan(fields, precision="fp64", out_dtype=np.float64, graph=True, device=dev)
+    for _ in range(3):
+        plan64.run(stream)
     torch.cuda.synchronize()
-    k64 = max(2, args.steps // 4)
+    k64 = max(3, args.steps // 4)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(k64):
-        step(_lib.FB_FP64, ws64, outs64, 1)
+        plan64.run(stream)
     e1.record(stream)
     torch.cuda.synchronize()
     fp64_value = W * H * B * k64 / (e0.elapsed_time(e1) / 1e3) / 1e6
-    q32 = torch.empty((H, W), dtype=torch.float64, device=dev)
-    L.fb_interpolate(0, prec, 2, d_pts[0].data_ptr(), d_val[0].data_ptr(), NPTS, c_sigma, c_x0, c_step, c_size,
-                     NITER, mdw, q32.data_ptr(), 1, ws.data_ptr(), ws.numel(), sptr)
+    planq = BatchPlan(fields, precision=args.precision, out_dtype=np.float64, graph=False, knobs=knobs, device=dev)
+    planq.run(stream)
     torch.cuda.synchronize()
-    a, b = q32.cpu().numpy(), outs64[0].cpu().numpy()
-    mm = ~np.isnan(a) & ~np.isnan(b)
-    err_rel = float(np.max(np.abs(a[mm] - b[mm])) / np.max(np.abs(b[mm])))
-    err_range = float(np.max(np.abs(a[mm] - b[mm])) / np.ptp(fields[0][1]))
-    mask_mismatch = int(np.sum(np.isnan(a) != np.isnan(b)))
-    del outs64, ws64
+    err_rel = err_range = 0.0
+    mask_mismatch = 0
+    for f in range(B):
+        a, b = planq.outs[f].cpu().numpy(), plan64.outs[f].cpu().numpy()
+        mm = ~np.isnan(a) & ~np.isnan(b)
+        err_rel = max(err_rel, float(np.max(np.abs(a[mm] - b[mm])) / np.max(np.abs(b[mm]))))
+        err_range = max(err_range, float(np.max(np.abs(a[mm] - b[mm])) / np.ptp(host[f][1])))
+        mask_mismatch += int(np.sum(np.isnan(a) != np.isnan(b)))
+    planq.close()
+    plan64.close()
 
-    # ---- e2e: C-ABI host entry from pinned host memory --------------------
+    # ---- one call per field (fb_interpolate), inputs resident -----------------
+    d = _lib.dvec
+    c_sigma, c_x0, c_step = d([SIGMA, SIGMA]), d(list(X0)), d(list(STEP))
+    c_size = d([W, H], ctypes.c_int64)
+    mdw = math.exp(-MAX_DIST ** 2 / 2)
+    need = ctypes.c_size_t(0)
+    _lib.check(L.fb_workspace_size(0, prec, 2, NPTS, c_sigma, c_step, c_size, NITER, ctypes.byref(need)))
+    ws = torch.empty(need.value, dtype=torch.uint8, device=dev)
+    sptr = ctypes.c_void_p(stream.cuda_stream)
+
+    def single_step():
+        for f in range(B):
+            _lib.check(L.fb_interpolate(0, prec, 2, fields[f]["pts"].data_ptr(), fields[f]["val"].data_ptr(), NPTS,
+                                        c_sigma, c_x0, c_step, c_size, NITER, mdw, plan.outs[f].data_ptr(), 0,
+                                        ws.data_ptr(), ws.numel(), sptr), "fb_interpolate")
+
+    for _ in range(3):
+        single_step()
+    torch.cuda.synchronize()
+    k1 = max(3, args.steps // 4)
+    e0.record(stream)
+    for _ in range(k1):
+        single_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    single_value = W * H * B * k1 / (e0.elapsed_time(e1) / 1e3) / 1e6
+    del ws
+
+    # ---- e2e: C-ABI host-buffer batch entry from pinned host memory --------
     h_pts = [L.fb_host_alloc(NPTS * 16) for _ in range(B)]
     h_val = [L.fb_host_alloc(NPTS * 8) for _ in range(B)]
     h_out = [L.fb_host_alloc(W * H * 4) for _ in range(B)]
     for f in range(B):
-        ctypes.memmove(h_pts[f], fields[f][0].ctypes.data, NPTS * 16)
-        ctypes.memmove(h_val[f], fields[f][1].ctypes.data, NPTS * 8)
+        ctypes.memmove(h_pts[f], host[f][0].ctypes.data, NPTS * 16)
+        ctypes.memmove(h_val[f], host[f][1].ctypes.data, NPTS * 8)
+    a_pts = (ctypes.c_void_p * B)(*h_pts)
+    a_val = (ctypes.c_void_p * B)(*h_val)
+    a_out = (ctypes.c_void_p * B)(*h_out)
 
     def e2e_step():
-        for f in range(B):
-            rc = L.fb_interpolate_host(0, prec, 2, h_pts[f], h_val[f], NPTS, c_sigma, c_x0, c_step, c_size, NITER,
-                                       mdw, h_out[f], 0, sptr)
-            if rc != 0:
-                _lib.check(rc, "fb_interpolate_host")
+        _lib.check(L.fb_batch_run_host(plan._h, a_pts, a_val, a_out, sptr), "fb_batch_run_host")
 
-    for _ in range(2):
+    for _ in range(3):
         e2e_step()
-    k_e2e = max(2, args.steps // 4)
+    k_e2e = max(3, args.steps // 2)
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(k_e2e):
         e2e_step()
     t_e2e = max_over_ranks(world, time.perf_counter() - t0)
     e2e_value = W * H * B * k_e2e * world / t_e2e / 1e6
+    chk = np.ctypeslib.as_array(ctypes.cast(h_out[0], ctypes.POINTER(ctypes.c_float)), shape=(H, W)).copy()
+    e2e_ok = bool(np.array_equal(chk, plan.outs[0].cpu().numpy(), equal_nan=True))
     for p in h_pts + h_val + h_out:
         L.fb_host_free(p)
-    L.fb_release()
+    plan.close()
 
     # ---- CPU baseline (rank 0, N = 1 only) ----------------------------------
     cpu = None
@@ -347,15 +380,15 @@ def main():
         cpu = {"value": rate, "unit": "Mgridpts/s", "cores": 1, "kind": "port",
                "sample": f"{nf} field(s) of {W}x{H}, N={NPTS}, float64, single thread, {secs:.1f} s"}
 
-    # bin keys, scan, bin scatter, bin sort, large-bin sort, two axis launches
-    launches_per_field = 5 + 2
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "Mgridpts/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec == _lib.FB_FP32C else "f64",
                 "data": "synthetic (seeded uniform samples, smooth field + noise)",
-                "config": workload_config(B, args.precision) | {"parallelism": f"replicas x{world}"},
-                "gpu_launches": launches_per_field * B * args.steps,
+                "config": workload_config(B, args.precision) | {"parallelism": f"replicas x{world}",
+                                                                 "knobs": {"chunk": knobs[0],
+                                                                           "rows_threads": knobs[1]}},
+                "gpu_launches": launches_per_step * args.steps,
                 "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
                              "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                              "traffic": None, "algorithmic_bytes_per_launch": alg[dom],
@@ -364,9 +397,14 @@ def main():
                              "pipeline_gbs": pipeline_gbs, "pipeline_frac": pipeline_gbs / peak},
                 "fp64_form": {"value": fp64_value, "unit": "Mgridpts/s", "speedup_of_fp32c": value / fp64_value},
                 "error_vs_fp64": {"rel_max": err_rel, "max_over_range": err_range, "mask_mismatch": mask_mismatch},
+                "single_call_form": {"value": single_value, "unit": "Mgridpts/s",
+                                     "entry": "fb_interpolate once per field, inputs resident"},
                 "e2e": {"value": e2e_value, "unit": "Mgridpts/s", "h2d_bytes_per_step": B * NPTS * 24,
-                        "d2h_bytes_per_step": B * W * H * 4, "entry": "fb_interpolate_host (pinned host buffers)"},
-                "cpu_baseline": cpu, "clocks": clk.summary()}
+                        "d2h_bytes_per_step": B * W * H * 4, "matches_device_result": e2e_ok,
+                        "entry": "fb_batch_run_host (pinned host buffers)"},
+                "cpu_baseline": cpu, "clocks": clk.summary(),
+                "plan": {"kernel_launches_per_step": launches_per_step, "memsets_per_step": memsets_per_step,
+                         "device_bytes": plan_bytes}}
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist

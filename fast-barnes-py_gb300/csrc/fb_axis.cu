@@ -29,6 +29,17 @@ static int chunk_k(int precision, int T)
 
 static bool direct_mode(int precision, int T) { return T <= (precision == 0 ? DirectMax<double>::T : DirectMax<float>::T); }
 
+// Chunk length of one launch: the direct-sum kernels and float64 use the
+// short chunk; a plan may pin 17 or 33 for float32 sliding sums.
+static int kchunk_of(int precision, int T, int kchunk)
+{
+    if (precision == 0 || direct_mode(precision, T) || T <= 32)
+        return K64;
+    if (kchunk == K64 || kchunk == K32)
+        return kchunk;
+    return chunk_k(precision, T);
+}
+
 static int cell_size(int precision) { return precision == 0 ? 16 : 8; }
 static int col_g(int precision) { return 32 / cell_size(precision); }
 int axis_col_group(int precision) { return col_g(precision); }
@@ -67,13 +78,13 @@ int axis_threads(int precision, const AxisLaunch &a)
     return col_g(precision) * a.chunks_pad;
 }
 
-AxisPlanLimits axis_limits(int precision, int T)
+AxisPlanLimits axis_limits(int precision, int T, int kchunk)
 {
     // the longest extent a rows-layout CTA (one line) and a columns-layout CTA
     // (G lines) can hold; the plan uses the one of its layout
     AxisPlanLimits l;
     l.smem_limit = axis_smem_limit();
-    const int K = chunk_k(precision, T);
+    const int K = kchunk_of(precision, T, kchunk);
     int best[2] = {0, 0};
     for (int lay = 0; lay < 2; lay++) {
         int lo = 1, hi = kMaxThreads * K;
@@ -101,7 +112,7 @@ AxisPlanLimits axis_limits(int precision, int T)
 
 bool axis_shape(int precision, AxisLaunch &a)
 {
-    const int K = chunk_k(precision, a.T);
+    const int K = kchunk_of(precision, a.T, a.kchunk);
     int64_t E = a.tile_len + 2 * (int64_t)a.halo;
     if (E > a.L)
         E = a.L;
@@ -114,8 +125,9 @@ bool axis_shape(int precision, AxisLaunch &a)
         a.lines_per_cta = col_g(precision);
         return axis_threads(precision, a) <= kMaxThreads && axis_smem_bytes(precision, a) <= axis_smem_limit();
     }
-    // rows: ~256 threads per CTA
-    int nl = std::max(1, std::min<int>(std::max(1, 256 / a.chunks_pad), kMaxThreads / a.chunks_pad));
+    // rows: ~256 threads per CTA unless the plan asks for another target
+    const int target = a.rows_threads > 0 ? a.rows_threads : 256;
+    int nl = std::max(1, std::min<int>(std::max(1, target / a.chunks_pad), kMaxThreads / a.chunks_pad));
     if (nl > a.nlines)
         nl = (int)a.nlines;
     for (; nl >= 1; nl--) {
@@ -131,6 +143,25 @@ cudaError_t launch_axis_f32(int k, int mode, int sd, const AxisLaunch &a, const 
 cudaError_t launch_axis_f64(int mode, int sd, const AxisLaunch &a, const Geometry &g, const SampleView &sv,
                             cudaStream_t st);
 
+cudaError_t launch_axis_batch_f32(int op, int k, int mode, int sd, int layout, const BatchAxisField *fields,
+                                  const BatchItem *items, uint32_t nitems, uint32_t *counter, size_t smem,
+                                  int threads, int *grid, cudaStream_t st);
+cudaError_t launch_axis_batch_f64(int op, int mode, int sd, int layout, const BatchAxisField *fields,
+                                  const BatchItem *items, uint32_t nitems, uint32_t *counter, size_t smem,
+                                  int threads, int *grid, cudaStream_t st);
+
+int axis_kernel_k(int precision, const AxisLaunch &a) { return kchunk_of(precision, a.T, a.kchunk); }
+int axis_kernel_mode(int precision, int T) { return direct_mode(precision, T) ? 1 : 0; }
+
+cudaError_t launch_axis_batch(int op, int precision, int k, int mode, int sd, int layout,
+                              const BatchAxisField *fields, const BatchItem *items, uint32_t nitems,
+                              uint32_t *counter, size_t smem, int threads, int *grid, cudaStream_t st)
+{
+    if (precision == 0)
+        return launch_axis_batch_f64(op, mode, sd, layout, fields, items, nitems, counter, smem, threads, grid, st);
+    return launch_axis_batch_f32(op, k, mode, sd, layout, fields, items, nitems, counter, smem, threads, grid, st);
+}
+
 cudaError_t launch_axis(int precision, const AxisLaunch &a, const Geometry &g, const SampleView &sv,
                         cudaStream_t st)
 {
@@ -140,7 +171,7 @@ cudaError_t launch_axis(int precision, const AxisLaunch &a, const Geometry &g, c
     const int mode = direct_mode(precision, a.T) ? 1 : 0;
     if (precision == 0)
         return launch_axis_f64(mode, sd, a, g, sv, st);
-    return launch_axis_f32(mode == 1 ? K64 : chunk_k(precision, a.T), mode, sd, a, g, sv, st);
+    return launch_axis_f32(kchunk_of(precision, a.T, a.kchunk), mode, sd, a, g, sv, st);
 }
 
 int axis_tune(const char *name, int value)

@@ -735,15 +735,6 @@ __global__ void __launch_bounds__(512, 1) k_axis(const AxisLaunch a, const Geome
 // field's launch) from a counter until none is left, largest fields first, so
 // fields of uneven size share the GPU without a tail per field.  No CTA waits
 // for another: each item is independent.
-struct BatchAxisField {
-    AxisLaunch a;
-    Geometry g;
-    SampleView sv;
-};
-struct BatchItem {
-    uint32_t field;
-    uint32_t block;
-};
 
 template <typename Real, int K, int MODE, int SPLAT_DIM, int LAYOUT>
 __global__ void __launch_bounds__(512, 1) k_axis_batch(const BatchAxisField *__restrict__ fields,
@@ -806,6 +797,51 @@ static cudaError_t launch_k(int sd, const AxisLaunch &a, const Geometry &g, cons
     case 2: return launch_one<Real, K, MODE, 2, 0>(a, g, sv, st);
     default: return launch_one<Real, K, MODE, 3, 0>(a, g, sv, st);
     }
+}
+
+template <typename Real, int K, int MODE, int SD, int LAY>
+static cudaError_t launch_batch_one(int op, const BatchAxisField *fields, const BatchItem *items, uint32_t nitems,
+                                    uint32_t *counter, size_t smem, int threads, int *grid, cudaStream_t st)
+{
+    if (op == 1) {
+        if (*grid < 1)
+            return cudaSuccess;
+        k_axis_batch<Real, K, MODE, SD, LAY><<<(unsigned)*grid, threads, smem, st>>>(fields, items, nitems, counter);
+        return cudaGetLastError();
+    }
+    cudaError_t e = cudaFuncSetAttribute(k_axis_batch<Real, K, MODE, SD, LAY>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)axis_smem_limit());
+    int per_sm = 0, dev = 0, sms = 0;
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_axis_batch<Real, K, MODE, SD, LAY>, threads,
+                                                          smem);
+    if (e == cudaSuccess)
+        e = cudaGetDevice(&dev);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess)
+        return e;
+    if (per_sm < 1)
+        return cudaErrorInvalidConfiguration;
+    *grid = (int)std::min<int64_t>((int64_t)per_sm * sms, (int64_t)nitems);
+    return cudaSuccess;
+}
+
+template <typename Real, int K, int MODE>
+static cudaError_t launch_batch_k(int op, int sd, int layout, const BatchAxisField *fields, const BatchItem *items,
+                                  uint32_t nitems, uint32_t *counter, size_t smem, int threads, int *grid,
+                                  cudaStream_t st)
+{
+#define FBG_B(SD, LAY) launch_batch_one<Real, K, MODE, SD, LAY>(op, fields, items, nitems, counter, smem, threads, grid, st)
+    if (layout == 1)
+        return FBG_B(0, 1);
+    switch (sd) {
+    case 0: return FBG_B(0, 0);
+    case 1: return FBG_B(1, 0);
+    case 2: return FBG_B(2, 0);
+    default: return FBG_B(3, 0);
+    }
+#undef FBG_B
 }
 
 }  // namespace fbg

@@ -10,7 +10,9 @@
 #include <string.h>
 
 #include <algorithm>
+#include <map>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "../../include/fastbarnes_gb300.h"
@@ -120,7 +122,8 @@ void axis_params(int method, double sigma, double step, int n, int &T, double &a
 }
 
 int make_plan(int method, int precision, int dim, int64_t npts, const double *sigma, const double *x0,
-              const double *step, const int64_t *size, int num_iter, double max_dist_weight, Plan &p)
+              const double *step, const int64_t *size, int num_iter, double max_dist_weight, Plan &p,
+              int kchunk = 0, int rows_threads = 0)
 {
     if (dim < 1 || dim > 3)
         return fail(FB_ERR_ARG, "dim must be 1, 2 or 3 (got %d)", dim);
@@ -192,7 +195,7 @@ int make_plan(int method, int precision, int dim, int64_t npts, const double *si
     for (int m = 0; m < dim; m++) {
         const int64_t L = size[m];
         const int T = g.T[m];
-        const AxisPlanLimits lim = axis_limits(precision, T);
+        const AxisPlanLimits lim = axis_limits(precision, T, kchunk);
         const int64_t emax = m == 0 ? lim.extent_max : lim.extent_max_cols;
         std::vector<AxisLaunch> axl;
         AxisLaunch a{};
@@ -209,6 +212,8 @@ int make_plan(int method, int precision, int dim, int64_t npts, const double *si
         a.alpha = g.alpha[m];
         a.scaled = scaled ? 1 : 0;
         a.inv_norm = inv[m];
+        a.kchunk = kchunk;
+        a.rows_threads = rows_threads;
         bool ok = false;
         if (L <= emax) {
             a.tile_len = L;
@@ -695,4 +700,551 @@ extern "C" int fb_resample(const float *d_lam, int64_t lam_w, int64_t lam_h, con
     cudaError_t e = launch_resample(d_lam, lam_w, lam_h, lam_x0, x0, step, size, proj, d_out, d_tab,
                                     (cudaStream_t)stream);
     return e == cudaSuccess ? FB_OK : cuda_fail(e, "resample");
+}
+
+// ---------------------------------------------------------------------------
+// batched 2D fields: one sample sort and one persistent launch per axis stage
+// for all fields of a plan
+// ---------------------------------------------------------------------------
+
+namespace {
+
+// One persistent launch: the same-shaped axis launches (kernel variant) of
+// several fields, as a table of BatchAxisField and a list of work items.
+struct BatchStage {
+    int k = 0, mode = 0, sd = 0, layout = 0, axis = 0;
+    size_t smem = 0;
+    int threads = 0;
+    int grid = 0;
+    size_t off_fields = 0, off_items = 0;
+    uint32_t nitems = 0;
+};
+
+std::mutex g_batch_tune_mu;
+std::map<std::string, fb_batch_knobs> g_batch_tuned;
+
+}  // namespace
+
+struct fb_batch {
+    int precision = 1, out_f64 = 0, flags = 0, device = 0;
+    fb_batch_knobs knobs{0, 0};
+    int nfields = 0;
+    int64_t ntot = 0;
+    uint32_t nbins = 0, nblocks = 0;
+    char *dev = nullptr;
+    size_t dev_bytes = 0;
+    size_t off_keyf = 0, off_blocks = 0, off_hdrs = 0, off_bins = 0, off_sort = 0, off_counters = 0;
+    std::vector<BatchStage> stages;
+    std::vector<fb_field2d> fields;
+    cudaStream_t cap = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+void batch_free(fb_batch *b)
+{
+    if (b->exec)
+        cudaGraphExecDestroy(b->exec);
+    if (b->graph)
+        cudaGraphDestroy(b->graph);
+    if (b->cap)
+        cudaStreamDestroy(b->cap);
+    if (b->dev)
+        cudaFree(b->dev);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    b->cap = nullptr;
+    b->dev = nullptr;
+}
+
+int batch_build(int precision, const fb_field2d *fields, int nf, int out_f64, fb_batch_knobs kn, fb_batch *b)
+{
+    if (nf < 1 || !fields)
+        return fail(FB_ERR_ARG, "a batch needs at least one field");
+    if (kn.chunk != 0 && kn.chunk != 17 && kn.chunk != 33)
+        return fail(FB_ERR_ARG, "chunk must be 0, 17 or 33 (got %d)", kn.chunk);
+    if (kn.rows_threads != 0 && kn.rows_threads != 128 && kn.rows_threads != 256 && kn.rows_threads != 512)
+        return fail(FB_ERR_ARG, "rows_threads must be 0, 128, 256 or 512 (got %d)", kn.rows_threads);
+    b->precision = precision;
+    b->out_f64 = out_f64 ? 1 : 0;
+    b->knobs = kn;
+    b->nfields = nf;
+    b->fields.assign(fields, fields + nf);
+    std::vector<Plan> plans((size_t)nf);
+    int64_t ntot = 0, nbins = 0;
+    std::vector<int64_t> sample_off((size_t)nf), bin_off((size_t)nf);
+    for (int f = 0; f < nf; f++) {
+        const fb_field2d &F = fields[f];
+        int rc = make_plan(F.method, precision, 2, F.n_pts, F.sigma, F.x0, F.step, F.size, F.num_iter,
+                           F.max_dist_weight, plans[f], kn.chunk, kn.rows_threads);
+        if (rc != FB_OK) {
+            char msg[sizeof(g_err)];
+            snprintf(msg, sizeof(msg), "%s", g_err);
+            return fail(rc, "field %d: %s", f, msg);
+        }
+        if (!F.out || (F.n_pts > 0 && (!F.pts || !F.val)))
+            return fail(FB_ERR_ARG, "field %d: null device pointer", f);
+        sample_off[f] = ntot;
+        bin_off[f] = nbins;
+        ntot += F.n_pts;
+        nbins += plans[f].nbins;
+    }
+    if (ntot > (int64_t)0xFFFFFFF0ll)
+        return fail(FB_ERR_ARG, "batch has too many samples (%lld)", (long long)ntot);
+    if (nbins > (int64_t)0xFFFFFFF0ll)
+        return fail(FB_ERR_ARG, "batch has too many grid rows (%lld)", (long long)nbins);
+    b->ntot = ntot;
+    b->nbins = (uint32_t)nbins;
+
+    // sample blocks of the bin-key kernel
+    std::vector<uint2> blocks;
+    for (int f = 0; f < nf; f++)
+        for (int64_t s0 = 0; s0 < fields[f].n_pts; s0 += kBatchKeysPerBlock)
+            blocks.push_back(make_uint2((unsigned)f, (unsigned)s0));
+    b->nblocks = (uint32_t)blocks.size();
+
+    // stages: the s-th launch of every field, grouped by kernel variant;
+    // within a group the fields with most work come first
+    size_t nstage_max = 0;
+    for (const Plan &p : plans)
+        nstage_max = std::max(nstage_max, p.launches.size());
+    struct Member {
+        int f;
+        size_t q;
+        int64_t blocks;
+    };
+    struct Group {
+        BatchStage st;
+        std::vector<Member> m;
+    };
+    std::vector<Group> groups;
+    for (size_t q = 0; q < nstage_max; q++) {
+        std::vector<Group> gs;
+        for (int f = 0; f < nf; f++) {
+            if (q >= plans[f].launches.size())
+                continue;
+            const AxisLaunch &a = plans[f].launches[q];
+            BatchStage key;
+            key.k = axis_kernel_k(precision, a);
+            key.mode = axis_kernel_mode(precision, a.T);
+            key.sd = a.fill_splat ? 2 : 0;
+            key.layout = a.layout;
+            key.axis = a.axis;
+            Group *g = nullptr;
+            for (Group &x : gs)
+                if (x.st.k == key.k && x.st.mode == key.mode && x.st.sd == key.sd && x.st.layout == key.layout)
+                    g = &x;
+            if (!g) {
+                gs.push_back(Group{key, {}});
+                g = &gs.back();
+            }
+            const int64_t grp = a.layout == 0 ? (a.nlines + a.lines_per_cta - 1) / a.lines_per_cta
+                                              : a.outer_count * a.xblocks;
+            g->m.push_back(Member{f, q, grp * a.ntiles});
+            g->st.smem = std::max(g->st.smem, axis_smem_bytes(precision, a));
+            g->st.threads = std::max(g->st.threads, axis_threads(precision, a));
+        }
+        for (Group &g : gs) {
+            std::stable_sort(g.m.begin(), g.m.end(),
+                             [](const Member &x, const Member &y) { return x.blocks > y.blocks; });
+            int64_t items = 0;
+            for (const Member &m : g.m)
+                items += m.blocks;
+            if (items > (int64_t)0xFFFFFFF0ll)
+                return fail(FB_ERR_ARG, "batch stage too large");
+            g.st.nitems = (uint32_t)items;
+            groups.push_back(g);
+        }
+    }
+
+    // device layout
+    const size_t sz = precision == FB_FP64 ? 8 : 4;
+    size_t off = 0;
+    b->off_keyf = off;
+    off = align_up(off + sizeof(BatchKeyField) * (size_t)nf);
+    b->off_blocks = off;
+    off = align_up(off + sizeof(uint2) * std::max<size_t>(1, blocks.size()));
+    b->off_hdrs = off;
+    off = align_up(off + sizeof(FieldHeader) * (size_t)nf);
+    b->off_bins = off;
+    off = align_up(off + sizeof(uint32_t) * ((size_t)nbins + 1));
+    b->off_sort = off;
+    off = align_up(off + batch_sort_scratch_bytes(ntot, (uint32_t)nbins, precision));
+    b->off_counters = off;
+    off = align_up(off + sizeof(uint32_t) * groups.size());
+    for (Group &g : groups) {
+        g.st.off_fields = off;
+        off = align_up(off + sizeof(BatchAxisField) * g.m.size());
+        g.st.off_items = off;
+        off = align_up(off + sizeof(BatchItem) * std::max<size_t>(1, g.st.nitems));
+    }
+    const size_t tables_end = off;
+    std::vector<size_t> pair_off((size_t)nf);
+    std::vector<size_t> pair_bytes((size_t)nf);
+    for (int f = 0; f < nf; f++) {
+        pair_off[f] = off;
+        pair_bytes[f] = align_up(2 * sz * (size_t)plans[f].npoints);
+        off += (size_t)plans[f].pairs * pair_bytes[f];
+    }
+    b->dev_bytes = off;
+    cudaError_t e = cudaGetDevice(&b->device);
+    if (e == cudaSuccess)
+        e = cudaMalloc(&b->dev, b->dev_bytes);
+    if (e != cudaSuccess) {
+        b->dev = nullptr;
+        return cuda_fail(e, "batch plan memory");
+    }
+    char *dv = b->dev;
+
+    // host image of the tables
+    std::vector<char> img(tables_end, 0);
+    BatchKeyField *kf = reinterpret_cast<BatchKeyField *>(img.data() + b->off_keyf);
+    for (int f = 0; f < nf; f++) {
+        const fb_field2d &F = fields[f];
+        kf[f].pts = F.pts;
+        kf[f].val = F.val;
+        kf[f].npts = F.n_pts;
+        kf[f].sample_offset = sample_off[f];
+        kf[f].bin_offset = (uint32_t)bin_off[f];
+        kf[f].pad = 0;
+        for (int m = 0; m < 2; m++) {
+            kf[f].x0[m] = F.x0[m];
+            kf[f].step[m] = F.step[m];
+            kf[f].size[m] = F.size[m];
+        }
+    }
+    if (!blocks.empty())
+        memcpy(img.data() + b->off_blocks, blocks.data(), sizeof(uint2) * blocks.size());
+    const uint32_t *sorted = nullptr;
+    const void *recs = nullptr;
+    batch_sort_views(precision, ntot, (uint32_t)nbins, reinterpret_cast<uint32_t *>(dv + b->off_sort), &sorted,
+                     &recs);
+    b->stages.clear();
+    for (size_t gi = 0; gi < groups.size(); gi++) {
+        Group &g = groups[gi];
+        BatchAxisField *tf = reinterpret_cast<BatchAxisField *>(img.data() + g.st.off_fields);
+        BatchItem *it = reinterpret_cast<BatchItem *>(img.data() + g.st.off_items);
+        uint32_t ni = 0;
+        for (size_t mi = 0; mi < g.m.size(); mi++) {
+            const Member &m = g.m[mi];
+            const Plan &p = plans[m.f];
+            AxisLaunch a = p.launches[m.q];
+            auto pair = [&](const void *code) -> void * {
+                const int idx = (int)(intptr_t)code - 16;
+                return idx < 0 ? nullptr : dv + pair_off[m.f] + (size_t)idx * pair_bytes[m.f];
+            };
+            a.src_v = pair(a.src_v);
+            a.dst_v = pair(a.dst_v);
+            a.src_w = nullptr;
+            a.dst_w = nullptr;
+            a.out = fields[m.f].out;
+            a.out_f64 = b->out_f64;
+            BatchAxisField &bf = tf[mi];
+            bf.a = a;
+            bf.g = p.g;
+            SampleView sv{};
+            sv.rec = recs;
+            sv.npts = ntot;
+            sv.sorted_idx = sorted;
+            sv.bin_start = reinterpret_cast<const uint32_t *>(dv + b->off_bins) + bin_off[m.f];
+            sv.nbins = p.nbins;
+            sv.bin_w = p.bin_w;
+            sv.hdr = reinterpret_cast<FieldHeader *>(dv + b->off_hdrs) + m.f;
+            bf.sv = sv;
+            for (int64_t k = 0; k < m.blocks; k++)
+                it[ni++] = BatchItem{(uint32_t)mi, (uint32_t)k};
+        }
+        BatchStage st = g.st;
+        e = launch_axis_batch(0, precision, st.k, st.mode, st.sd, st.layout, nullptr, nullptr, st.nitems, nullptr,
+                              st.smem, st.threads, &st.grid, nullptr);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "batch axis kernel setup");
+        b->stages.push_back(st);
+    }
+    e = cudaMemcpy(dv, img.data(), tables_end, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "batch tables upload");
+    return FB_OK;
+}
+
+int batch_enqueue(fb_batch *b, cudaStream_t st, bool prof)
+{
+    char *dv = b->dev;
+    size_t ev = prof ? prof_event(st) : 0;
+    cudaError_t e = cudaMemsetAsync(dv + b->off_counters, 0, sizeof(uint32_t) * std::max<size_t>(1, b->stages.size()),
+                                    st);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "batch counters");
+    const uint32_t *sorted = nullptr;
+    const void *recs = nullptr;
+    e = batch_sort(b->precision, reinterpret_cast<const BatchKeyField *>(dv + b->off_keyf),
+                   reinterpret_cast<const uint2 *>(dv + b->off_blocks), b->nblocks, b->ntot, b->nbins,
+                   reinterpret_cast<FieldHeader *>(dv + b->off_hdrs), b->nfields,
+                   reinterpret_cast<uint32_t *>(dv + b->off_sort), reinterpret_cast<uint32_t *>(dv + b->off_bins),
+                   &sorted, &recs, st);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "batch sample sort");
+    if (prof) {
+        size_t e1 = prof_event(st);
+        g_prof.recs.push_back({0, ev, e1});
+        ev = e1;
+    }
+    uint32_t *counters = reinterpret_cast<uint32_t *>(dv + b->off_counters);
+    for (size_t i = 0; i < b->stages.size(); i++) {
+        BatchStage &s = b->stages[i];
+        e = launch_axis_batch(1, b->precision, s.k, s.mode, s.sd, s.layout,
+                              reinterpret_cast<const BatchAxisField *>(dv + s.off_fields),
+                              reinterpret_cast<const BatchItem *>(dv + s.off_items), s.nitems, counters + i, s.smem,
+                              s.threads, &s.grid, st);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "batch axis kernel");
+        if (prof) {
+            size_t e1 = prof_event(st);
+            g_prof.recs.push_back({1 + s.axis, ev, e1});
+            ev = e1;
+        }
+    }
+    return FB_OK;
+}
+
+std::string batch_signature(int precision, const fb_field2d *fields, int nf, int out_f64)
+{
+    std::string sig;
+    char buf[256];
+    snprintf(buf, sizeof(buf), "p%d o%d n%d", precision, out_f64, nf);
+    sig += buf;
+    for (int f = 0; f < nf; f++) {
+        const fb_field2d &F = fields[f];
+        snprintf(buf, sizeof(buf), "|%d %lld %lld %d %d %d %lld", F.method, (long long)F.size[0],
+                 (long long)F.size[1], fb_half_kernel_size_opt(F.sigma[0], F.step[0], F.num_iter),
+                 fb_half_kernel_size_opt(F.sigma[1], F.step[1], F.num_iter), F.num_iter, (long long)F.n_pts);
+        sig += buf;
+    }
+    return sig;
+}
+
+// Times each candidate launch shape on the given fields (2 warm-up runs,
+// best of 5) and returns the fastest.
+int batch_tune(int precision, const fb_field2d *fields, int nf, int out_f64, fb_batch_knobs *best)
+{
+    bool wide = false;
+    for (int f = 0; f < nf && precision == FB_FP32C; f++)
+        for (int m = 0; m < 2; m++)
+            if (fb_half_kernel_size_opt(fields[f].sigma[m], fields[f].step[m], fields[f].num_iter) > 32)
+                wide = true;
+    std::vector<int> chunks = wide ? std::vector<int>{17, 33} : std::vector<int>{0};
+    const int rows[3] = {128, 256, 512};
+    cudaStream_t st = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&e0);
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&e1);
+    float best_ms = 1e30f;
+    *best = fb_batch_knobs{0, 0};
+    int rc = e == cudaSuccess ? FB_OK : cuda_fail(e, "tuning stream");
+    for (int c : chunks) {
+        for (int r : rows) {
+            if (rc != FB_OK)
+                break;
+            fb_batch tb;
+            rc = batch_build(precision, fields, nf, out_f64, fb_batch_knobs{c, r}, &tb);
+            float t_best = 1e30f;
+            for (int it = 0; rc == FB_OK && it < 7; it++) {
+                if (it >= 2)
+                    cudaEventRecord(e0, st);
+                rc = batch_enqueue(&tb, st, false);
+                if (rc == FB_OK && it >= 2) {
+                    cudaEventRecord(e1, st);
+                    e = cudaEventSynchronize(e1);
+                    float ms = 0.f;
+                    if (e == cudaSuccess)
+                        e = cudaEventElapsedTime(&ms, e0, e1);
+                    if (e != cudaSuccess)
+                        rc = cuda_fail(e, "tuning run");
+                    t_best = std::min(t_best, ms);
+                }
+            }
+            if (rc == FB_OK && t_best < best_ms) {
+                best_ms = t_best;
+                *best = fb_batch_knobs{c, r};
+            }
+            cudaStreamSynchronize(st);
+            batch_free(&tb);
+        }
+    }
+    if (e0)
+        cudaEventDestroy(e0);
+    if (e1)
+        cudaEventDestroy(e1);
+    if (st)
+        cudaStreamDestroy(st);
+    return rc;
+}
+
+}  // namespace
+
+extern "C" int fb_batch_create(int precision, const fb_field2d *fields, int n_fields, int out_f64, int flags,
+                               const fb_batch_knobs *knobs, fb_batch **plan)
+{
+    g_err[0] = 0;
+    if (!plan)
+        return fail(FB_ERR_ARG, "plan pointer is required");
+    *plan = nullptr;
+    if (precision != FB_FP64 && precision != FB_FP32C)
+        return fail(FB_ERR_ARG, "unknown precision %d", precision);
+    if (flags & ~(FB_BATCH_GRAPH | FB_BATCH_TUNE))
+        return fail(FB_ERR_ARG, "unknown batch flags 0x%x", flags);
+    fb_batch_knobs kn{0, 0};
+    if (knobs) {
+        kn = *knobs;
+    } else if (flags & FB_BATCH_TUNE) {
+        if (n_fields < 1 || !fields)
+            return fail(FB_ERR_ARG, "a batch needs at least one field");
+        const std::string sig = batch_signature(precision, fields, n_fields, out_f64);
+        std::lock_guard<std::mutex> lk(g_batch_tune_mu);
+        auto it = g_batch_tuned.find(sig);
+        if (it != g_batch_tuned.end()) {
+            kn = it->second;
+        } else {
+            int rc = batch_tune(precision, fields, n_fields, out_f64, &kn);
+            if (rc != FB_OK)
+                return rc;
+            g_batch_tuned[sig] = kn;
+        }
+    }
+    fb_batch *b = new fb_batch();
+    b->flags = flags;
+    int rc = batch_build(precision, fields, n_fields, out_f64, kn, b);
+    if (rc == FB_OK && (flags & FB_BATCH_GRAPH)) {
+        cudaError_t e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking);
+        if (e != cudaSuccess)
+            rc = cuda_fail(e, "batch capture stream");
+    }
+    if (rc != FB_OK) {
+        batch_free(b);
+        delete b;
+        return rc;
+    }
+    *plan = b;
+    return FB_OK;
+}
+
+extern "C" int fb_batch_run(fb_batch *b, void *stream)
+{
+    g_err[0] = 0;
+    if (!b)
+        return fail(FB_ERR_ARG, "null plan");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!(b->flags & FB_BATCH_GRAPH)) {
+        std::unique_lock<std::mutex> plk(g_prof.mu, std::defer_lock);
+        const bool prof = g_prof.on;
+        if (prof)
+            plk.lock();
+        return batch_enqueue(b, st, prof);
+    }
+    if (!b->exec) {
+        cudaError_t e = cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "batch graph capture");
+        int rc = batch_enqueue(b, b->cap, false);
+        cudaGraph_t g = nullptr;
+        e = cudaStreamEndCapture(b->cap, &g);
+        if (rc != FB_OK) {
+            if (g)
+                cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess)
+            return cuda_fail(e, "batch graph capture");
+        b->graph = g;
+        e = cudaGraphInstantiate(&b->exec, g, 0);
+        if (e != cudaSuccess) {
+            b->exec = nullptr;
+            return cuda_fail(e, "batch graph instantiate");
+        }
+    }
+    cudaError_t e = cudaGraphLaunch(b->exec, st);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "batch graph launch");
+    return FB_OK;
+}
+
+extern "C" int fb_batch_run_host(fb_batch *b, const double *const *h_pts, const double *const *h_val,
+                                 void *const *h_out, void *stream)
+{
+    g_err[0] = 0;
+    if (!b || !h_pts || !h_val || !h_out)
+        return fail(FB_ERR_ARG, "null argument");
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaSuccess;
+    for (int f = 0; f < b->nfields && e == cudaSuccess; f++) {
+        const fb_field2d &F = b->fields[f];
+        if (F.n_pts == 0)
+            continue;
+        if (!h_pts[f] || !h_val[f])
+            return fail(FB_ERR_ARG, "field %d: null host pointer", f);
+        e = cudaMemcpyAsync((void *)F.pts, h_pts[f], sizeof(double) * 2 * (size_t)F.n_pts, cudaMemcpyHostToDevice,
+                            st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync((void *)F.val, h_val[f], sizeof(double) * (size_t)F.n_pts, cudaMemcpyHostToDevice,
+                                st);
+    }
+    if (e != cudaSuccess)
+        return cuda_fail(e, "batch inputs to device");
+    int rc = fb_batch_run(b, stream);
+    if (rc != FB_OK)
+        return rc;
+    const size_t osz = b->out_f64 ? 8 : 4;
+    for (int f = 0; f < b->nfields && e == cudaSuccess; f++) {
+        const fb_field2d &F = b->fields[f];
+        if (!h_out[f])
+            return fail(FB_ERR_ARG, "field %d: null host pointer", f);
+        e = cudaMemcpyAsync(h_out[f], F.out, osz * (size_t)F.size[0] * (size_t)F.size[1], cudaMemcpyDeviceToHost,
+                            st);
+    }
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "batch results to host");
+    return FB_OK;
+}
+
+extern "C" int fb_batch_knobs_of(const fb_batch *b, fb_batch_knobs *knobs)
+{
+    if (!b || !knobs)
+        return fail(FB_ERR_ARG, "null argument");
+    *knobs = b->knobs;
+    return FB_OK;
+}
+
+extern "C" int fb_batch_info(const fb_batch *b, int *kernel_launches, int *memsets, size_t *device_bytes)
+{
+    if (!b)
+        return fail(FB_ERR_ARG, "null plan");
+    // batch_sort: k_batch_keys (when there are samples), k_tile_sums,
+    // k_scan_exclusive, k_tile_scan, then k_bin_scatter, k_sort_bins,
+    // k_sort_large when there are samples; two memsets; plus the counters'
+    // memset and one persistent launch per stage with work
+    int k = 3 + (b->nblocks > 0 ? 1 : 0) + (b->ntot > 0 ? 3 : 0);
+    for (const BatchStage &s : b->stages)
+        k += s.grid > 0 ? 1 : 0;
+    if (kernel_launches)
+        *kernel_launches = k;
+    if (memsets)
+        *memsets = 3;
+    if (device_bytes)
+        *device_bytes = b->dev_bytes;
+    return FB_OK;
+}
+
+extern "C" void fb_batch_destroy(fb_batch *b)
+{
+    if (!b)
+        return;
+    batch_free(b);
+    delete b;
 }

@@ -155,6 +155,21 @@ struct AxisLaunch {
     const void *src_v, *src_w;
     void *dst_v, *dst_w;
     void *out;
+    // planning choices (host side only)
+    int kchunk;               // chunk length: 0 = automatic, 17 or 33
+    int rows_threads;         // rows layout: target threads per CTA (0 = 256)
+};
+
+// One field of a batched axis launch, and one CTA's share of work in it
+// (a line group / tile of that field).
+struct BatchAxisField {
+    AxisLaunch a;
+    Geometry g;
+    SampleView sv;
+};
+struct BatchItem {
+    uint32_t field;
+    uint32_t block;
 };
 
 }  // namespace fbg

@@ -11,6 +11,9 @@ cudaError_t sort_samples(int precision, const double *pts, const double *val, in
                          const uint32_t **sorted_idx, const void **recs, cudaStream_t st);
 
 size_t batch_sort_scratch_bytes(int64_t ntot, uint32_t nbins, int precision);
+// The sorted-index and record arrays batch_sort leaves in its scratch.
+void batch_sort_views(int precision, int64_t ntot, uint32_t nbins, uint32_t *scratch, const uint32_t **sorted_idx,
+                      const void **recs);
 cudaError_t batch_sort(int precision, const BatchKeyField *d_fields, const uint2 *d_blocks, uint32_t nblocks,
                        int64_t ntot, uint32_t nbins, FieldHeader *hdrs, int nfields, uint32_t *scratch,
                        uint32_t *bin_start, const uint32_t **sorted_idx, const void **recs, cudaStream_t st);
@@ -22,7 +25,7 @@ struct AxisPlanLimits {
     size_t smem_limit;     // dynamic shared memory per block
 };
 // Longest line extent one CTA holds for half kernel width T.
-AxisPlanLimits axis_limits(int precision, int T);
+AxisPlanLimits axis_limits(int precision, int T, int kchunk = 0);
 // Lines per columns-layout CTA: 32 bytes of (v, w) cells per grid row.
 int axis_col_group(int precision);
 // Shared memory needed by one CTA of a launch.
@@ -32,6 +35,17 @@ size_t axis_smem_bytes(int precision, const AxisLaunch &a);
 bool axis_shape(int precision, AxisLaunch &a);
 cudaError_t launch_axis(int precision, const AxisLaunch &a, const Geometry &g, const SampleView &sv,
                         cudaStream_t st);
+// Batched launches (structures in fb_axis_impl.cuh).
+struct BatchAxisField;
+struct BatchItem;
+int axis_kernel_k(int precision, const AxisLaunch &a);
+int axis_kernel_mode(int precision, int T);
+int axis_threads(int precision, const AxisLaunch &a);
+// op 0: set the kernel's shared-memory limit and return in *grid the
+// persistent grid (resident CTAs x SMs, at most nitems); op 1: launch it.
+cudaError_t launch_axis_batch(int op, int precision, int k, int mode, int sd, int layout,
+                              const BatchAxisField *fields, const BatchItem *items, uint32_t nitems,
+                              uint32_t *counter, size_t smem, int threads, int *grid, cudaStream_t st);
 // Tuning knobs ("chunk": 0 automatic, 17 or 33); returns 0 if accepted.
 int axis_tune(const char *name, int value);
 // Standalone n-pass box filter over contiguous device lines (no splat, no

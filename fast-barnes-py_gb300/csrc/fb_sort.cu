@@ -416,6 +416,15 @@ size_t batch_sort_scratch_bytes(int64_t ntot, uint32_t nbins, int precision)
     return sort_scratch_bytes(ntot, nbins, precision) + 8 * tiles + 256;
 }
 
+void batch_sort_views(int precision, int64_t ntot, uint32_t nbins, uint32_t *scratch, const uint32_t **sorted_idx,
+                      const void **recs)
+{
+    const size_t words = 3 * ((size_t)nbins + 2) + 4 * (size_t)ntot;
+    *sorted_idx = scratch + 3 * ((size_t)nbins + 2) + (size_t)ntot;
+    *recs = reinterpret_cast<char *>(scratch) + (4 * words + 255) / 256 * 256;
+    (void)precision;
+}
+
 cudaError_t batch_sort(int precision, const BatchKeyField *d_fields, const uint2 *d_blocks, uint32_t nblocks,
                        int64_t ntot, uint32_t nbins, FieldHeader *hdrs, int nfields, uint32_t *scratch,
                        uint32_t *bin_start, const uint32_t **sorted_idx, const void **recs, cudaStream_t st)

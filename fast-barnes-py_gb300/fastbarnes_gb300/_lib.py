@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libfastbarnes_gb300.so")
 
 FB_OK = 0
-FB_ERR_KERNEL_SIZE = 2
+FB_ERR_ARG, FB_ERR_KERNEL_SIZE = 1, 2
 FB_FP64, FB_FP32C = 0, 1
 FB_OPTIMIZED_CONVOLUTION, FB_CONVOLUTION = 0, 1
 
@@ -21,6 +21,31 @@ PRECISIONS = {"fp64": FB_FP64, "float64": FB_FP64, "fp32c": FB_FP32C}
 
 _lib = None
 _lock = threading.Lock()
+
+
+class Field2D(ctypes.Structure):
+    """fb_field2d: one field of a batch (device pointers, grid, parameters)."""
+    _fields_ = [
+        ("pts", ctypes.c_void_p),
+        ("val", ctypes.c_void_p),
+        ("n_pts", ctypes.c_int64),
+        ("sigma", ctypes.c_double * 2),
+        ("x0", ctypes.c_double * 2),
+        ("step", ctypes.c_double * 2),
+        ("size", ctypes.c_int64 * 2),
+        ("num_iter", ctypes.c_int),
+        ("max_dist_weight", ctypes.c_double),
+        ("method", ctypes.c_int),
+        ("out", ctypes.c_void_p),
+    ]
+
+
+class BatchKnobs(ctypes.Structure):
+    """fb_batch_knobs: launch shape of a batch plan."""
+    _fields_ = [("chunk", ctypes.c_int), ("rows_threads", ctypes.c_int)]
+
+
+FB_BATCH_GRAPH, FB_BATCH_TUNE = 1, 2
 
 
 class FastBarnesError(RuntimeError):
@@ -72,6 +97,13 @@ def lib():
             "fb_tune": ([ctypes.c_char_p, i], i),
             "fb_profile_begin": ([], i),
             "fb_profile_end": ([P, P, i, ctypes.POINTER(i)], i),
+            "fb_batch_create": ([i, ctypes.POINTER(Field2D), i, i, i, ctypes.POINTER(BatchKnobs),
+                                 ctypes.POINTER(P)], i),
+            "fb_batch_run": ([P, P], i),
+            "fb_batch_run_host": ([P, P, P, P, P], i),
+            "fb_batch_knobs_of": ([P, ctypes.POINTER(BatchKnobs)], i),
+            "fb_batch_info": ([P, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(sz)], i),
+            "fb_batch_destroy": ([P], None),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)

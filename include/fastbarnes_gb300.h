@@ -108,6 +108,64 @@ void fb_release(void);
 int fb_profile_begin(void);
 int fb_profile_end(int *stages, float *ms, int max_records, int *n_records);
 
+/* ---- batched 2D fields ------------------------------------------------------
+ * No reference counterpart: the reference interpolates one field per call
+ * (fastbarnes/interpolation.py:36 barnes; a batch is a Python loop over it,
+ * demo/timing1_table1_figure4.py:107-115).  A plan holds many independent 2D
+ * fields (each its own samples, sigma, grid and output, optimized convolution
+ * or convolution) and runs all of them with one sample sort and one persistent
+ * launch per axis.  Every field's result equals that of fb_interpolate on it.
+ *
+ * fb_batch_create checks the fields, plans the launches and allocates the
+ * plan's device memory (tables, sort scratch, intermediate fields) on the
+ * current device.  The device pointers in `fields` are kept: fb_batch_run
+ * reads pts / val and writes out of every field each time (refill the input
+ * buffers between runs to interpolate new data).  flags:
+ *   FB_BATCH_GRAPH  capture the run's launches in a CUDA graph at the first
+ *                   fb_batch_run and replay it afterwards;
+ *   FB_BATCH_TUNE   time the candidate launch shapes on the given fields at
+ *                   creation (runs the batch; inputs must be valid) and keep
+ *                   the fastest; the choice is remembered for identical
+ *                   batches in this process.
+ * knobs (optional) pins the launch shape instead; fb_batch_knobs_of reports
+ * the one in use. */
+typedef struct fb_field2d {
+    const double *pts;        /* device, n_pts x 2 */
+    const double *val;        /* device, n_pts */
+    int64_t n_pts;
+    double sigma[2], x0[2], step[2];
+    int64_t size[2];          /* (nx, ny); out is ny x nx */
+    int num_iter;
+    double max_dist_weight;
+    int method;               /* FB_OPTIMIZED_CONVOLUTION or FB_CONVOLUTION */
+    void *out;                /* device, float32 (or float64 with out_f64) */
+} fb_field2d;
+
+typedef struct fb_batch_knobs {
+    int chunk;                /* 0 automatic, 17 or 33 (float32 windows wider than 65) */
+    int rows_threads;         /* x-axis threads per CTA target: 0 (= 256), 128, 256 or 512 */
+} fb_batch_knobs;
+
+typedef struct fb_batch fb_batch;
+
+enum { FB_BATCH_GRAPH = 1, FB_BATCH_TUNE = 2 };
+
+int fb_batch_create(int precision, const fb_field2d *fields, int n_fields, int out_f64, int flags,
+                    const fb_batch_knobs *knobs, fb_batch **plan);
+/* Enqueues the whole batch on `stream` (0 = the legacy default stream). */
+int fb_batch_run(fb_batch *plan, void *stream);
+/* Host-buffer form: copies h_pts[f] (n_pts x 2) and h_val[f] of every field
+ * into the plan's device inputs, runs the batch and copies every output into
+ * h_out[f] (size[1] x size[0]); returns when the results are in host memory.
+ * Pinned host buffers (fb_host_alloc) make the copies asynchronous. */
+int fb_batch_run_host(fb_batch *plan, const double *const *h_pts, const double *const *h_val, void *const *h_out,
+                      void *stream);
+int fb_batch_knobs_of(const fb_batch *plan, fb_batch_knobs *knobs);
+/* Kernel launches and memsets one fb_batch_run enqueues, and the plan's
+ * device bytes. */
+int fb_batch_info(const fb_batch *plan, int *kernel_launches, int *memsets, size_t *device_bytes);
+void fb_batch_destroy(fb_batch *plan);
+
 /* ---- the 1D rect-kernel passes alone -----------------------------------------
  * Replaces _accumulate_tail_array (interpolation.py:484-533; rect_len = 2T+1,
  * tail weight alpha) and _accumulate_array (:729-772; alpha = 0): num_iter

@@ -123,3 +123,33 @@ def test_workspace_scales_with_plan():
     assert need64.value >= 2 * 4096 * 2048 * 8
     assert need32.value >= 2 * 4096 * 2048 * 4
     assert need32.value < need64.value
+
+
+def test_batch_argument_errors_in_c_abi():
+    """fb_batch_create rejects bad batches before it touches a device."""
+    L = _lib.lib()
+    h = ctypes.c_void_p()
+    arr = (_lib.Field2D * 2)()
+    for F in arr:
+        F.pts, F.val, F.out, F.n_pts = 8, 8, 8, 10   # never dereferenced on these paths
+        F.sigma[:] = [1.0, 1.0]
+        F.x0[:] = [0.0, 0.0]
+        F.step[:] = [1 / 32, 1 / 32]
+        F.size[:] = [200, 100]
+        F.num_iter, F.max_dist_weight, F.method = 4, 0.002, 0
+    assert L.fb_batch_create(1, arr, 0, 0, 0, None, ctypes.byref(h)) == _lib.FB_ERR_ARG
+    assert b"at least one field" in L.fb_last_error()
+    assert L.fb_batch_create(1, arr, 2, 0, 8, None, ctypes.byref(h)) == _lib.FB_ERR_ARG
+    kn = _lib.BatchKnobs(5, 0)
+    assert L.fb_batch_create(1, arr, 2, 0, 0, ctypes.byref(kn), ctypes.byref(h)) == _lib.FB_ERR_ARG
+    assert b"chunk" in L.fb_last_error()
+    kn = _lib.BatchKnobs(0, 300)
+    assert L.fb_batch_create(1, arr, 2, 0, 0, ctypes.byref(kn), ctypes.byref(h)) == _lib.FB_ERR_ARG
+    arr[1].size[1] = 20   # 2T+1 = 65 >= 20
+    assert L.fb_batch_create(1, arr, 2, 0, 0, None, ctypes.byref(h)) == _lib.FB_ERR_KERNEL_SIZE
+    assert L.fb_last_error().startswith(b"field 1:")
+    arr[1].size[1] = 100
+    arr[0].out = None
+    assert L.fb_batch_create(1, arr, 2, 0, 0, None, ctypes.byref(h)) == _lib.FB_ERR_ARG
+    assert b"null device pointer" in L.fb_last_error()
+    assert h.value is None

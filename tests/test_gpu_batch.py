@@ -1,0 +1,132 @@
+"""GPU parity of the batched form (fb_batch_*): every field of a batch equals
+the single-field call on it, and the oracle within the stated tolerances.
+
+Tolerances: a batch runs the same kernels' arithmetic per field as the
+single-field path with the same launch shape, so with equal knobs the two are
+compared for exact equality (NaN positions included); against the oracle the
+FP64 form is within 1e-9 * max(|ref|, range(val)) and the FP32C form within
+1e-5 relative max error (see test_gpu_parity.py).
+"""
+import numpy as np
+import pytest
+
+from fastbarnes_gb300 import interpolation as I
+from fastbarnes_gb300.batched import BatchPlan, barnes_batch
+from oracle import oracle
+
+from test_gpu_parity import check_fp32c, check_fp64
+
+pytestmark = pytest.mark.gpu
+
+
+def uneven_fields(torch, seed=7):
+    """Fields of different grids, sigma, n, sample counts and methods,
+    including a 20000-cell row that the x axis must tile."""
+    rng = np.random.default_rng(seed)
+    specs = [
+        dict(N=6000, sigma=1.0, x0=(-26.0, 34.5), step=1 / 32, size=(1200, 600), n=4, method="optimized_convolution"),
+        dict(N=300, sigma=0.4, x0=(0.0, 0.0), step=0.1, size=(130, 90), n=3, method="optimized_convolution"),
+        dict(N=2500, sigma=(0.01, 0.004), x0=(0.0, 0.0), step=1e-3, size=(20000, 64), n=3,
+             method="optimized_convolution"),
+        dict(N=4000, sigma=0.8, x0=(-5.0, -3.0), step=(0.05, 0.04), size=(400, 350), n=5, method="convolution"),
+        dict(N=1, sigma=0.3, x0=(0.0, 0.0), step=0.1, size=(40, 30), n=4, method="optimized_convolution"),
+    ]
+    fields, host = [], []
+    for s in specs:
+        size = s["size"]
+        step = np.broadcast_to(np.asarray(s["step"], float), (2,))
+        lo = np.asarray(s["x0"]) - 2 * step
+        hi = np.asarray(s["x0"]) + step * (np.asarray(size) + 2)
+        pts = rng.uniform(lo, hi, (s["N"], 2))
+        val = 50 + 10 * np.sin(pts[:, 0] * 3) + rng.normal(0, 1, s["N"])
+        host.append((pts, val, s))
+        fields.append(dict(pts=torch.as_tensor(pts, device="cuda"), val=torch.as_tensor(val, device="cuda"),
+                           sigma=s["sigma"], x0=s["x0"], step=s["step"], size=size, num_iter=s["n"],
+                           method=s["method"]))
+    return fields, host
+
+
+def single(pts, val, s, precision, out_dtype=np.float64):
+    return I.barnes(pts, val, s["sigma"], s["x0"], s["step"], s["size"], method=s["method"], num_iter=s["n"],
+                    precision=precision, out_dtype=out_dtype)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+@pytest.mark.parametrize("graph", [False, True])
+def test_batch_equals_single(precision, graph):
+    import torch
+    fields, host = uneven_fields(torch)
+    plan = BatchPlan(fields, precision=precision, out_dtype=np.float64, graph=graph)
+    for rep in range(2):
+        outs = [o.cpu().numpy() for o in plan.run()]
+        for (pts, val, s), o in zip(host, outs):
+            ref = single(pts, val, s, precision)
+            assert o.shape == ref.shape
+            assert np.array_equal(o, ref, equal_nan=True), (s, rep)
+    plan.close()
+
+
+def test_batch_refill_inputs():
+    """New data written into the plan's input tensors is picked up by the
+    next run (graph replay included)."""
+    import torch
+    fields, host = uneven_fields(torch, seed=8)
+    plan = BatchPlan(fields, precision="fp32c", out_dtype=np.float64, graph=True)
+    plan.run()
+    rng = np.random.default_rng(99)
+    for k, (pts, val, s) in enumerate(host):
+        nv = val[::-1].copy() + rng.normal(0, 1, len(val))
+        plan.val[k].copy_(torch.as_tensor(nv))
+        host[k] = (pts, nv, s)
+    outs = [o.cpu().numpy() for o in plan.run()]
+    for (pts, val, s), o in zip(host, outs):
+        assert np.array_equal(o, single(pts, val, s, "fp32c"), equal_nan=True)
+    plan.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_batch_vs_oracle(precision):
+    import torch
+    fields, host = uneven_fields(torch, seed=9)
+    outs = barnes_batch(fields, precision=precision, out_dtype=np.float64)
+    outs32 = barnes_batch(fields, precision=precision)
+    for (pts, val, s), q, q32 in zip(host, outs, outs32):
+        ref_out, ref_q, wg, thr = oracle.interpolate(pts, val, s["sigma"], s["x0"], s["step"], s["size"], s["n"],
+                                                     method=s["method"], nthreads=8)
+        q = q.cpu().numpy()
+        if precision == "fp64":
+            check_fp64(q, q32.cpu().numpy(), ref_q, ref_out, wg, thr, val)
+        else:
+            check_fp32c(q, ref_q, wg, thr)
+
+
+def test_batch_headline_shape_knobs_and_tuning():
+    """Eight 1024 x 512 fields with a window wider than 65 cells: every pinned
+    launch shape and the tuned one stay within the FP32C bound of the oracle
+    and agree with the single-field call for equal knobs."""
+    import torch
+    rng = np.random.default_rng(4)
+    B, N = 3, 20000
+    size, step, x0, sigma = (1024, 512), 1 / 64, (0.0, 0.0), 1.0
+    host = []
+    for b in range(B):
+        pts = rng.uniform(0, [16, 8], (N, 2))
+        val = 280 + 15 * np.cos(pts[:, 0] / 3 + b) + rng.normal(0, 1, N)
+        host.append((pts, val))
+    fields = [dict(pts=torch.as_tensor(p, device="cuda"), val=torch.as_tensor(v, device="cuda"), sigma=sigma, x0=x0,
+                   step=step, size=size, num_iter=4) for p, v in host]
+    refs = [oracle.interpolate(p, v, sigma, x0, step, size, 4, nthreads=8) for p, v in host]
+    seen = set()
+    for knobs in ((17, 128), (33, 256), (33, 512), None):
+        plan = BatchPlan(fields, precision="fp32c", out_dtype=np.float64, graph=True, tune=knobs is None,
+                         knobs=knobs)
+        got = plan.knobs
+        assert got[0] in (17, 33) and got[1] in (128, 256, 512)
+        seen.add(got)
+        outs = [o.cpu().numpy() for o in plan.run()]
+        for (p, v), (ref_out, ref_q, wg, thr), o in zip(host, refs, outs):
+            check_fp32c(o, ref_q, wg, thr)
+        launches, memsets, nbytes = plan.info
+        assert launches == 9 and memsets == 3 and nbytes > 0
+        plan.close()
+    assert len(seen) >= 3
