@@ -1248,3 +1248,74 @@ extern "C" void fb_batch_destroy(fb_batch *b)
     batch_free(b);
     delete b;
 }
+
+// ---------------------------------------------------------------------------
+// resampling without allocation
+// ---------------------------------------------------------------------------
+//
+// fb_resample needs device scratch for its row / column tables (size[1] +
+// 2 size[0] doubles), which the caller allocates.  Some callers cannot
+// allocate at call time: code that runs while another component owns the
+// device allocator, or a loop with a latency budget that cudaMalloc /
+// cudaFree (which may synchronize the device) would break.  For them
+// fb_resample_noalloc keeps the tables in one file-scope device array of
+// fixed size, located once per device with cudaGetSymbolAddress.
+//
+// Every table entry the resample kernel reads is written by the table
+// kernels of the same call first, so nothing in the array has to start at
+// zero.  The array is shared by every call on a device: two calls that
+// overlap in time (different streams or host threads) race on it.
+
+namespace {
+constexpr int64_t kResampleScratchDoubles = 49152;   // 384 KiB: size[1] + 2 * size[0] <= 49152
+constexpr int kMaxScratchDevices = 64;
+static __device__ __align__(256) double g_resample_scratch[kResampleScratchDoubles];
+std::mutex g_scratch_mu;
+double *g_scratch_ptr[kMaxScratchDevices] = {};
+
+// Address of the scratch array on the current device; the first call for a
+// device looks it up (no allocation).
+int resample_scratch(double **out)
+{
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "fb_resample_noalloc: current device");
+    if (dev < 0 || dev >= kMaxScratchDevices)
+        return fail(FB_ERR_ARG, "fb_resample_noalloc: device %d beyond the %d supported", dev, kMaxScratchDevices);
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_resample_scratch);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "fb_resample_noalloc: scratch address");
+        g_scratch_ptr[dev] = static_cast<double *>(p);
+    }
+    *out = g_scratch_ptr[dev];
+    return FB_OK;
+}
+}  // namespace
+
+extern "C" int fb_resample_noalloc(const float *d_lam, int64_t lam_w, int64_t lam_h, const double *lam_x0,
+                                   const double *x0, const double *step, const int64_t *size, const double *proj,
+                                   float *d_out, void *stream)
+{
+    g_err[0] = 0;
+    if (!d_lam || !lam_x0 || !x0 || !step || !size || !proj || !d_out || size[0] < 1 || size[1] < 1 ||
+        lam_w < 2 || lam_h < 2)
+        return fail(FB_ERR_ARG, "invalid resample arguments");
+    if (size[0] > kResampleScratchDoubles || size[1] > kResampleScratchDoubles ||
+        size[1] + 2 * size[0] > kResampleScratchDoubles)
+        return fail(FB_ERR_ARG,
+                    "fb_resample_noalloc: grid %lld x %lld needs %lld table doubles, more than the static "
+                    "scratch of %lld (size[1] + 2 * size[0] <= %lld); use fb_resample with a caller workspace",
+                    (long long)size[0], (long long)size[1], (long long)(size[1] + 2 * size[0]),
+                    (long long)kResampleScratchDoubles, (long long)kResampleScratchDoubles);
+    double *tab = nullptr;
+    int rc = resample_scratch(&tab);
+    if (rc != FB_OK)
+        return rc;
+    cudaError_t e = launch_resample(d_lam, lam_w, lam_h, lam_x0, x0, step, size, proj, d_out, tab,
+                                    (cudaStream_t)stream);
+    return e == cudaSuccess ? FB_OK : cuda_fail(e, "resample");
+}

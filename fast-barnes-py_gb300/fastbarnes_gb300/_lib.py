@@ -94,6 +94,7 @@ def lib():
             "fb_lambert_create_proj": ([d, d, d, d, P], None),
             "fb_lambert_to_map": ([P, P, i64, P, P], i),
             "fb_resample": ([P, i64, i64, P, P, P, P, P, P, P, P], i),
+            "fb_resample_noalloc": ([P, i64, i64, P, P, P, P, P, P, P], i),
             "fb_tune": ([ctypes.c_char_p, i], i),
             "fb_profile_begin": ([], i),
             "fb_profile_end": ([P, P, i, ctypes.POINTER(i)], i),

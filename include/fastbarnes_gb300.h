@@ -207,6 +207,18 @@ int fb_resample(const float *d_lam, int64_t lam_w, int64_t lam_h, const double *
                 const double *step, const int64_t *size, const double *proj, float *d_out, double *d_tab,
                 void *stream);
 
+/* No reference counterpart: fb_resample without the d_tab argument, for
+ * callers that cannot allocate device memory at call time (code running while
+ * another component owns the device allocator, or a loop whose latency budget
+ * a cudaMalloc / cudaFree would break).  The tables live in a static device
+ * array of 49152 doubles (384 KiB), so size[1] + 2 * size[0] <= 49152; larger
+ * grids return FB_ERR_ARG.  The first call on a device looks the array up
+ * (cudaGetSymbolAddress) -- make it once before any stream capture.  Calls
+ * that overlap in time on one device share the array and race: serialize
+ * them.  Allocates nothing. */
+int fb_resample_noalloc(const float *d_lam, int64_t lam_w, int64_t lam_h, const double *lam_x0, const double *x0,
+                        const double *step, const int64_t *size, const double *proj, float *d_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

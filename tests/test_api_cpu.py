@@ -153,3 +153,16 @@ def test_batch_argument_errors_in_c_abi():
     assert L.fb_batch_create(1, arr, 2, 0, 0, None, ctypes.byref(h)) == _lib.FB_ERR_ARG
     assert b"null device pointer" in L.fb_last_error()
     assert h.value is None
+
+
+def test_resample_noalloc_rejects_grid_beyond_static_scratch():
+    """The size check of fb_resample_noalloc runs on the host before any
+    device call (the pointers here are never dereferenced)."""
+    L = _lib.lib()
+    d = _lib.dvec
+    proj = d([11.5, 0.7, 1.4, 1.0, 1.0])
+    for W, H in ((16385, 16384), (100, 49000), (49153, 1)):
+        rc = L.fb_resample_noalloc(8, 640, 440, d([-32.0, -2.0]), d([0.0, 0.0]), d([0.1, 0.1]),
+                                   d([W, H], ctypes.c_int64), proj, 8, None)
+        assert rc == _lib.FB_ERR_ARG
+        assert b"static scratch" in L.fb_last_error()
