@@ -281,11 +281,57 @@ def main():
     pipeline_bytes = B * (NPTS * 28 + W * H * (4 * sz + 4))
     pipeline_gbs = pipeline_bytes * args.steps / (t_ms / 1e3) / 1e9
 
+    # ---- one call per field (fb_interpolate), inputs resident -----------------
+    d = _lib.dvec
+    c_sigma, c_x0, c_step = d([SIGMA, SIGMA]), d(list(X0)), d(list(STEP))
+    c_size = d([W, H], ctypes.c_int64)
+    mdw = math.exp(-MAX_DIST ** 2 / 2)
+    need = ctypes.c_size_t(0)
+    _lib.check(L.fb_workspace_size(0, prec, 2, NPTS, c_sigma, c_step, c_size, NITER, ctypes.byref(need)))
+    ws = torch.empty(need.value, dtype=torch.uint8, device=dev)
+    sptr = ctypes.c_void_p(stream.cuda_stream)
+    if knobs[0]:
+        _lib.check(L.fb_tune(b"chunk", knobs[0]), "fb_tune")
+
+    def single_step():
+        for f in range(B):
+            _lib.check(L.fb_interpolate(0, prec, 2, fields[f]["pts"].data_ptr(), fields[f]["val"].data_ptr(), NPTS,
+                                        c_sigma, c_x0, c_step, c_size, NITER, mdw, plan.outs[f].data_ptr(), 0,
+                                        ws.data_ptr(), ws.numel(), sptr), "fb_interpolate")
+
+    for _ in range(3):
+        single_step()
+    torch.cuda.synchronize()
+    k1 = max(3, args.steps // 4)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(k1):
+        single_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    single_value = W * H * B * k1 / (e0.elapsed_time(e1) / 1e3) / 1e6
+    _lib.check(L.fb_profile_begin())
+    single_step()
+    maxrec = 8 * B
+    st1 = (ctypes.c_int * maxrec)()
+    tm1 = (ctypes.c_float * maxrec)()
+    nr1 = ctypes.c_int(0)
+    _lib.check(L.fb_profile_end(st1, tm1, maxrec, ctypes.byref(nr1)))
+    single_stage = {}
+    for i in range(nr1.value):
+        single_stage.setdefault(st1[i], []).append(tm1[i])
+    single_stage_ms = {k: statistics.median(v) for k, v in single_stage.items()}
+    _lib.check(L.fb_tune(b"chunk", 0), "fb_tune")
+    del ws
+
     if args.quick:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": "Mgridpts/s", "quick": True,
                               "knobs": knobs, "ms_per_step": t_ms / args.steps,
-                              "stage_ms": {names[k]: v for k, v in stage_ms.items()}}), flush=True)
+                              "stage_ms": {names[k]: v for k, v in stage_ms.items()},
+                              "single_call_value": single_value,
+                              "single_call_stage_ms_per_field": {k: v for k, v in single_stage_ms.items()}}),
+                  flush=True)
         plan.close()
         return
 
@@ -315,34 +361,6 @@ def main():
         mask_mismatch += int(np.sum(np.isnan(a) != np.isnan(b)))
     planq.close()
     plan64.close()
-
-    # ---- one call per field (fb_interpolate), inputs resident -----------------
-    d = _lib.dvec
-    c_sigma, c_x0, c_step = d([SIGMA, SIGMA]), d(list(X0)), d(list(STEP))
-    c_size = d([W, H], ctypes.c_int64)
-    mdw = math.exp(-MAX_DIST ** 2 / 2)
-    need = ctypes.c_size_t(0)
-    _lib.check(L.fb_workspace_size(0, prec, 2, NPTS, c_sigma, c_step, c_size, NITER, ctypes.byref(need)))
-    ws = torch.empty(need.value, dtype=torch.uint8, device=dev)
-    sptr = ctypes.c_void_p(stream.cuda_stream)
-
-    def single_step():
-        for f in range(B):
-            _lib.check(L.fb_interpolate(0, prec, 2, fields[f]["pts"].data_ptr(), fields[f]["val"].data_ptr(), NPTS,
-                                        c_sigma, c_x0, c_step, c_size, NITER, mdw, plan.outs[f].data_ptr(), 0,
-                                        ws.data_ptr(), ws.numel(), sptr), "fb_interpolate")
-
-    for _ in range(3):
-        single_step()
-    torch.cuda.synchronize()
-    k1 = max(3, args.steps // 4)
-    e0.record(stream)
-    for _ in range(k1):
-        single_step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    single_value = W * H * B * k1 / (e0.elapsed_time(e1) / 1e3) / 1e6
-    del ws
 
     # ---- e2e: C-ABI host-buffer batch entry from pinned host memory --------
     h_pts = [L.fb_host_alloc(NPTS * 16) for _ in range(B)]
@@ -398,7 +416,8 @@ def main():
                 "fp64_form": {"value": fp64_value, "unit": "Mgridpts/s", "speedup_of_fp32c": value / fp64_value},
                 "error_vs_fp64": {"rel_max": err_rel, "max_over_range": err_range, "mask_mismatch": mask_mismatch},
                 "single_call_form": {"value": single_value, "unit": "Mgridpts/s",
-                                     "entry": "fb_interpolate once per field, inputs resident"},
+                                     "entry": "fb_interpolate once per field, inputs resident",
+                                     "stage_ms_per_field": single_stage_ms},
                 "e2e": {"value": e2e_value, "unit": "Mgridpts/s", "h2d_bytes_per_step": B * NPTS * 24,
                         "d2h_bytes_per_step": B * W * H * 4, "matches_device_result": e2e_ok,
                         "entry": "fb_batch_run_host (pinned host buffers)"},

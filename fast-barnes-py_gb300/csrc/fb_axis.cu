@@ -59,13 +59,30 @@ size_t axis_smem_limit()
     return (size_t)lim;
 }
 
-static int pitch_of(int64_t E) { return (int)((E + 3) / 4 * 4); }
+static int even(int64_t x) { return (int)((x + 1) / 2 * 2); }
+
+// Shared-memory geometry of a launch whose longest line extent is E: chunk
+// slots, the line buffer with T + 1 zero cells before the line and zeros up
+// to T + 1 cells past the last chunk, and the partial-sum arrays with zero
+// slots for the ceil(T/K) chunks before and floor((T+1)/K) + 1 after.
+static void set_geometry(int precision, AxisLaunch &a, int K, int64_t E)
+{
+    const int nch = (int)((E + K - 1) / K);
+    const int unit = a.layout == 0 ? 32 : 32 / col_g(precision);
+    a.chunks_pad = (nch + unit - 1) / unit * unit;
+    a.extent_max = (int)E;
+    a.line_pad = a.T + 1;
+    a.line_pitch = even((int64_t)nch * K + 2 * (int64_t)a.line_pad);
+    const int d1 = (a.T + K - 1) / K, d2 = (a.T + 1) / K;
+    a.part_pad = d1;
+    a.part_pitch = even((int64_t)d1 + a.chunks_pad + d2 + 1);
+}
 
 size_t axis_smem_bytes(int precision, const AxisLaunch &a)
 {
     const size_t cs = cell_size(precision);
     const size_t nlc = a.layout == 0 ? (size_t)a.lines_per_cta : (size_t)col_g(precision);
-    size_t b = nlc * ((size_t)a.line_pitch + 3 * (size_t)a.chunks_pad) * cs;
+    size_t b = nlc * ((size_t)a.line_pitch + 3 * (size_t)a.part_pitch) * cs;
     if (a.fill_splat)
         b += nlc * kStage * (precision == 0 ? sizeof(StageRec<double>) : sizeof(StageRec<float>));
     return b;
@@ -87,17 +104,15 @@ AxisPlanLimits axis_limits(int precision, int T, int kchunk)
     const int K = kchunk_of(precision, T, kchunk);
     int best[2] = {0, 0};
     for (int lay = 0; lay < 2; lay++) {
-        int lo = 1, hi = kMaxThreads * K;
+        int lo = 0, hi = kMaxThreads * K;
         while (lo < hi) {
             int mid = (lo + hi + 1) / 2;
             AxisLaunch a{};
             a.layout = lay;
             a.lines_per_cta = 1;
             a.fill_splat = lay == 0;
-            a.line_pitch = pitch_of(mid);
-            const int nch = (mid + K - 1) / K;
-            const int unit = lay == 0 ? 32 : 32 / col_g(precision);
-            a.chunks_pad = (nch + unit - 1) / unit * unit;
+            a.T = T;
+            set_geometry(precision, a, K, mid);
             if (axis_threads(precision, a) <= kMaxThreads && axis_smem_bytes(precision, a) <= l.smem_limit)
                 lo = mid;
             else
@@ -116,11 +131,7 @@ bool axis_shape(int precision, AxisLaunch &a)
     int64_t E = a.tile_len + 2 * (int64_t)a.halo;
     if (E > a.L)
         E = a.L;
-    const int nch = (int)((E + K - 1) / K);
-    const int unit = a.layout == 0 ? 32 : 32 / col_g(precision);
-    a.chunks_pad = (nch + unit - 1) / unit * unit;
-    a.extent_max = (int)E;
-    a.line_pitch = pitch_of(E);
+    set_geometry(precision, a, K, E);
     if (a.layout == 1) {
         a.lines_per_cta = col_g(precision);
         return axis_threads(precision, a) <= kMaxThreads && axis_smem_bytes(precision, a) <= axis_smem_limit();

@@ -61,16 +61,29 @@ struct CellOf<double> {
 
 // float32 pairs: the packed .f32x2 instructions through CUDA's intrinsics
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+// a - b as one packed fma: b * -1 is exact, so the result is the rounded difference
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
 __device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+// float64 pairs: adds, subtracts and products through the _rn intrinsics, so
+// that the compiler never fuses a product into a following add (the splat's
+// w * v + cell would otherwise become an fma in some kernels and not in others)
+__device__ __forceinline__ double2 cadd(double2 a, double2 b)
+{
+    return make_double2(__dadd_rn(a.x, b.x), __dadd_rn(a.y, b.y));
+}
+__device__ __forceinline__ double2 csub(double2 a, double2 b)
+{
+    return make_double2(__dsub_rn(a.x, b.x), __dsub_rn(a.y, b.y));
+}
 __device__ __forceinline__ double2 cfma(double2 a, double2 b, double2 c)
 {
     return make_double2(fma(a.x, b.x, c.x), fma(a.y, b.y, c.y));
 }
-__device__ __forceinline__ double2 cmul(double2 a, double2 b) { return make_double2(a.x * b.x, a.y * b.y); }
+__device__ __forceinline__ double2 cmul(double2 a, double2 b)
+{
+    return make_double2(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y));
+}
 
 template <typename C>
 __device__ __forceinline__ C czero();
@@ -87,16 +100,10 @@ template <>
 __device__ __forceinline__ double2 csplat<double2>(double x) { return make_double2(x, x); }
 
 // ---------------------------------------------------------------------------
-// one line seen by one thread: cell e lives at s[e * ES]
+// one line seen by one thread: cell e lives at s[e * ES]; the line buffer has
+// zero cells on both sides (T + 1 before the line, up to the end of the last
+// chunk + T + 1 after it), so no read needs a bounds check
 // ---------------------------------------------------------------------------
-
-template <bool GUARD, int ES, typename C>
-__device__ __forceinline__ C rd(const C *__restrict__ s, int e, int E)
-{
-    if (GUARD)
-        return (unsigned)e < (unsigned)E ? s[e * ES] : czero<C>();
-    return s[e * ES];
-}
 
 template <typename C, bool SCALED>
 struct PassCoef {
@@ -113,37 +120,33 @@ struct PassCoef {
 // Slides the window over the chunk [k0, k0 + K): forward from A0 (window at
 // k0) over the first half, backward from A1 (window at k0 + K) over the rest;
 // the two halves are independent, so their steps are interleaved.
-template <typename C, int K, int ES, bool GUARD, bool SCALED>
-__device__ __forceinline__ void slide(const C *__restrict__ s, int E, int k0, int T, C A0, C A1,
+template <typename C, int K, int ES, bool SCALED>
+__device__ __forceinline__ void slide(const C *__restrict__ s, int k0, int T, C A0, C A1,
                                       const PassCoef<C, SCALED> &c, C (&o)[K])
 {
     constexpr int H = K / 2;   // forward steps 0 .. H-1, backward steps K-1 .. H
     C af = A0, ab = A1;
-    C prev = rd<GUARD, ES>(s, k0 - T - 1, E);
-    C odb = rd<GUARD, ES>(s, k0 + K - 1 - T, E);
+    const C *lo = s + (k0 - T - 1) * ES;   // cell k0 - T - 1
+    const C *hi = s + (k0 + T + 1) * ES;   // cell k0 + T + 1
+    C prev = lo[0];
+    C odb = lo[K * ES];                    // cell k0 + K - 1 - T
 #pragma unroll
     for (int i = 0; i < H; i++) {
-        const int kf = k0 + i;
-        const C nwf = rd<GUARD, ES>(s, kf + T + 1, E);
-        const C odf = rd<GUARD, ES>(s, kf - T, E);
-        const int kb = k0 + K - 1 - i;
-        const C nwb = rd<GUARD, ES>(s, kb + T + 1, E);
-        const C tlb = rd<GUARD, ES>(s, kb - T - 1, E);
+        const C nwf = hi[i * ES];                   // k0 + i + T + 1
+        const C odf = lo[(i + 1) * ES];             // k0 + i - T
+        const C nwb = hi[(K - 1 - i) * ES];         // kb + T + 1, kb = k0 + K - 1 - i
+        const C tlb = lo[(K - 1 - i) * ES];         // kb - T - 1
         o[i] = c.out(af, cadd(prev, nwf));
-        af = cadd(af, nwf);
-        af = csub(af, odf);
+        af = csub(cadd(af, nwf), odf);
         prev = odf;
-        ab = csub(ab, nwb);
-        ab = cadd(ab, odb);
+        ab = cadd(csub(ab, nwb), odb);
         o[K - 1 - i] = c.out(ab, cadd(tlb, nwb));
         odb = tlb;
     }
     {
-        const int kb = k0 + H;
-        const C nwb = rd<GUARD, ES>(s, kb + T + 1, E);
-        const C tlb = rd<GUARD, ES>(s, kb - T - 1, E);
-        ab = csub(ab, nwb);
-        ab = cadd(ab, odb);
+        const C nwb = hi[H * ES];
+        const C tlb = lo[H * ES];
+        ab = cadd(csub(ab, nwb), odb);
         o[H] = c.out(ab, cadd(tlb, nwb));
     }
 }
@@ -152,15 +155,15 @@ __device__ __forceinline__ void slide(const C *__restrict__ s, int E, int k0, in
 // K + 2T + 2 inputs the chunk needs, held in registers.  Sliding a window of
 // only a few cells over K/2 steps would carry the rounding error of large
 // values that have already left the window.
-template <typename C, int K, int ES, int TD, bool GUARD, bool SCALED>
-__device__ __forceinline__ void direct_pass(const C *__restrict__ s, int E, int k0, const PassCoef<C, SCALED> &c,
-                                            C (&o)[K])
+template <typename C, int K, int ES, int TD, bool SCALED>
+__device__ __forceinline__ void direct_pass(const C *__restrict__ s, int k0, const PassCoef<C, SCALED> &c, C (&o)[K])
 {
     constexpr int NX = K + 2 * TD + 2;
     C x[NX];
+    const C *lo = s + (k0 - TD - 1) * ES;
 #pragma unroll
     for (int m = 0; m < NX; m++)
-        x[m] = rd<GUARD, ES>(s, k0 - TD - 1 + m, E);
+        x[m] = lo[m * ES];
 #pragma unroll
     for (int i = 0; i < K; i++) {
         C acc = x[i + 1];
@@ -183,90 +186,112 @@ struct DirectMax<double> {
 };
 
 template <typename Real, typename C, int K, int ES, int TD, bool SCALED>
-__device__ __forceinline__ void direct_dispatch(int T, const C *s, int E, int k0, bool guard,
-                                                const PassCoef<C, SCALED> &c, C (&o)[K])
+__device__ __forceinline__ void direct_dispatch(int T, const C *s, int k0, const PassCoef<C, SCALED> &c, C (&o)[K])
 {
     if constexpr (TD <= DirectMax<Real>::T) {
         if (T != TD) {
-            direct_dispatch<Real, C, K, ES, TD + 1, SCALED>(T, s, E, k0, guard, c, o);
+            direct_dispatch<Real, C, K, ES, TD + 1, SCALED>(T, s, k0, c, o);
             return;
         }
-        if (guard)
-            direct_pass<C, K, ES, TD, true, SCALED>(s, E, k0, c, o);
-        else
-            direct_pass<C, K, ES, TD, false, SCALED>(s, E, k0, c, o);
+        direct_pass<C, K, ES, TD, SCALED>(s, k0, c, o);
     }
 }
 
 // Sums of a chunk that the next pass's anchors are built from: the whole
-// chunk (S), its first r2 cells (Pre) and its cells from r1 on (Suf).  Cells
-// at or beyond the line extent count as zero (tail chunk only).
-template <typename C, int K, bool TAIL>
-__device__ __forceinline__ void chunk_partials(const C (&o)[K], int k0, int E, int r1, int r2, C &S, C &Pre,
-                                               C &Suf)
+// chunk (S), its first R2 cells (Pre) and its cells from R1 on (Suf), as sums
+// of the (at most three) segments that R1 and R2 cut the chunk into.
+template <typename C, int K, int R1, int R2>
+__device__ __forceinline__ void partials_fixed(const C (&o)[K], C &S, C &Pre, C &Suf)
 {
-    C s = czero<C>(), p = czero<C>(), u = czero<C>();
+    constexpr int B0 = R1 < R2 ? R1 : R2, B1 = R1 < R2 ? R2 : R1;
+    C s0 = czero<C>(), s1 = czero<C>(), s2 = czero<C>();
 #pragma unroll
-    for (int i = 0; i < K; i++) {
-        const C x = (!TAIL || k0 + i < E) ? o[i] : czero<C>();
-        s = cadd(s, x);
-        if (i < r2)
-            p = cadd(p, x);
-        if (i >= r1)
-            u = cadd(u, x);
+    for (int i = 0; i < B0; i++)
+        s0 = cadd(s0, o[i]);
+#pragma unroll
+    for (int i = B0; i < B1; i++)
+        s1 = cadd(s1, o[i]);
+#pragma unroll
+    for (int i = B1; i < K; i++)
+        s2 = cadd(s2, o[i]);
+    S = cadd(cadd(s0, s1), s2);
+    if (R2 <= R1) {
+        Pre = s0;   // [0, R2)
+        Suf = s2;   // [R1, K)
+    } else {
+        Pre = cadd(s0, s1);   // [0, R1) + [R1, R2)
+        Suf = cadd(s1, s2);   // [R1, R2) + [R2, K)
     }
-    S = s;
-    Pre = p;
-    Suf = u;
 }
 
-template <int PS, typename C>
-__device__ __forceinline__ C part_at(const C *__restrict__ a, int m, int nch)
+// t = T mod K selects R1 = (K - t) mod K, R2 = (t + 1) mod K at compile time
+// (one indirect branch per pass, the same for every thread).
+template <typename C, int K>
+__device__ __forceinline__ void chunk_partials(const C (&o)[K], int t, C &S, C &Pre, C &Suf)
 {
-    return (unsigned)m < (unsigned)nch ? a[m * PS] : czero<C>();
+#define FBG_PC(TT)                                                                                                  \
+    case TT:                                                                                                        \
+        if constexpr (TT < K)                                                                                       \
+            partials_fixed<C, K, (K - TT) % K, (TT + 1) % K>(o, S, Pre, Suf);                                       \
+        break;
+    switch (t) {
+        FBG_PC(0) FBG_PC(1) FBG_PC(2) FBG_PC(3) FBG_PC(4) FBG_PC(5) FBG_PC(6) FBG_PC(7) FBG_PC(8) FBG_PC(9)
+        FBG_PC(10) FBG_PC(11) FBG_PC(12) FBG_PC(13) FBG_PC(14) FBG_PC(15) FBG_PC(16) FBG_PC(17) FBG_PC(18)
+        FBG_PC(19) FBG_PC(20) FBG_PC(21) FBG_PC(22) FBG_PC(23) FBG_PC(24) FBG_PC(25) FBG_PC(26) FBG_PC(27)
+        FBG_PC(28) FBG_PC(29) FBG_PC(30) FBG_PC(31) FBG_PC(32)
+    default: break;
+    }
+#undef FBG_PC
 }
+static_assert(K32 <= 33 && K64 <= 33, "chunk_partials lists t up to 32");
 
 // Window sums at k0 = jK and k0 + K from the chunk partials (T >= 1):
 // window [k0-T, k0+T] = Suf[m1] + S[m1+1 .. m2-1] + Pre[m2], m1 = j - d1,
 // m2 = j + d2 (d1 = ceil(T/K), d2 = floor((T+1)/K)).  Every term is a sum of
-// cells inside the window: nothing is subtracted.
+// cells inside the window: nothing is subtracted.  The partial arrays have
+// zero slots for the chunks before and after the line.
 template <int PS, typename C>
 __device__ __forceinline__ void anchors(const C *__restrict__ S, const C *__restrict__ Pre, const C *__restrict__ Suf,
-                                        int nch, int j, int d1, int d2, C &A0, C &A1)
+                                        int j, int d1, int d2, C &A0, C &A1)
 {
     const int m1 = j - d1, m2 = j + d2;
     C mid = czero<C>();
     for (int m = m1 + 2; m <= m2 - 1; m++)
-        mid = cadd(mid, part_at<PS>(S, m, nch));
+        mid = cadd(mid, S[m * PS]);
     const bool two = (m2 - m1) >= 2;
-    A0 = cadd(cadd(cadd(part_at<PS>(Suf, m1, nch), two ? part_at<PS>(S, m1 + 1, nch) : czero<C>()), mid),
-              part_at<PS>(Pre, m2, nch));
-    A1 = cadd(cadd(cadd(part_at<PS>(Suf, m1 + 1, nch), mid), two ? part_at<PS>(S, m2, nch) : czero<C>()),
-              part_at<PS>(Pre, m2 + 1, nch));
+    A0 = cadd(cadd(cadd(Suf[m1 * PS], two ? S[(m1 + 1) * PS] : czero<C>()), mid), Pre[m2 * PS]);
+    A1 = cadd(cadd(cadd(Suf[(m1 + 1) * PS], mid), two ? S[m2 * PS] : czero<C>()), Pre[(m2 + 1) * PS]);
+}
+
+// Outputs of the chunk at or beyond the line extent are not part of the line:
+// zero them so that the partial sums see the line's zeros there.
+template <typename C, int K>
+__device__ __forceinline__ void clip_tail(C (&o)[K], int k0, int E)
+{
+    if (k0 + K > E) {
+#pragma unroll
+        for (int i = 0; i < K; i++)
+            if (k0 + i >= E)
+                o[i] = czero<C>();
+    }
 }
 
 // One box pass of one thread's chunk: outputs into o, next partials into S/P/U.
 template <typename Real, typename C, int K, int ES, int PS, bool SCALED, bool DIRECT>
-__device__ __forceinline__ void run_pass(const C *__restrict__ ln, const C *__restrict__ pp, int QS, int E, int nch,
-                                         int j, int T, int d1, int d2, int r1, int r2,
-                                         const PassCoef<C, SCALED> &c, C (&o)[K], C &S, C &P, C &U)
+__device__ __forceinline__ void run_pass(const C *__restrict__ ln, const C *__restrict__ pp, int QS, int E, int j,
+                                         int T, int d1, int d2, int tk, const PassCoef<C, SCALED> &c, C (&o)[K],
+                                         C &S, C &P, C &U)
 {
     const int k0 = j * K;
-    const bool guard = (k0 - T - 1 < 0) || (k0 + K + T >= E);
     if constexpr (DIRECT) {
-        direct_dispatch<Real, C, K, ES, 0, SCALED>(T, ln, E, k0, guard, c, o);
+        direct_dispatch<Real, C, K, ES, 0, SCALED>(T, ln, k0, c, o);
         return;
     }
     C A0, A1;
-    anchors<PS>(pp, pp + QS, pp + 2 * QS, nch, j, d1, d2, A0, A1);
-    if (guard)
-        slide<C, K, ES, true, SCALED>(ln, E, k0, T, A0, A1, c, o);
-    else
-        slide<C, K, ES, false, SCALED>(ln, E, k0, T, A0, A1, c, o);
-    if (k0 + K <= E)
-        chunk_partials<C, K, false>(o, k0, E, r1, r2, S, P, U);
-    else
-        chunk_partials<C, K, true>(o, k0, E, r1, r2, S, P, U);
+    anchors<PS>(pp, pp + QS, pp + 2 * QS, j, d1, d2, A0, A1);
+    slide<C, K, ES, SCALED>(ln, k0, T, A0, A1, c, o);
+    clip_tail(o, k0, E);
+    chunk_partials<C, K>(o, tk, S, P, U);
 }
 
 // NaN where the weight is below the mask level, else vg / wg + offset
@@ -442,10 +467,13 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
     constexpr int ES = G;   // cell stride inside a line buffer
     constexpr int PS = G;   // chunk stride inside a partials array
     C *cells = reinterpret_cast<C *>(smem_raw);
-    const int P = a.line_pitch;
+    const int P = a.line_pitch;    // cells per line slot, zero pads included
+    const int HP = a.line_pad;     // zero cells before cell 0 of a line
     const int CP = a.chunks_pad;
+    const int PP = a.part_pitch;   // partial-sum slots per line, zero pads included
+    const int PF = a.part_pad;     // zero slots before chunk 0
     const int NLC = LAYOUT == 0 ? a.lines_per_cta : G;   // line slots in this CTA
-    C *part = cells + (size_t)NLC * P;                    // [3][NLC][CP] (rows) / [3][CP][G] (columns)
+    C *part = cells + (size_t)NLC * P;                    // [3][NLC][PP] (rows) / [3][PP][G] (columns)
     const int tid = threadIdx.x;
     const int nthr = blockDim.x;
 
@@ -479,24 +507,31 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
     if (LAYOUT == 0) {
         li = tid / CP;
         j = tid - li * CP;
-        ln = cells + (size_t)li * P;
-        QS = NLC * CP;
-        pp0 = part + (size_t)li * CP;
+        ln = cells + (size_t)li * P + HP;
+        QS = NLC * PP;
+        pp0 = part + (size_t)li * PP + PF;
     } else {
         j = tid / G;
         li = tid - j * G;
-        ln = cells + li;
-        QS = CP * G;
-        pp0 = part + li;
+        ln = cells + (size_t)HP * G + li;
+        QS = PP * G;
+        pp0 = part + (size_t)PF * G + li;
     }
     C *pw = const_cast<C *>(pp0) + (size_t)j * PS;   // this chunk's S slot
     const bool active = li < nl && j < nch;
     const int T = a.T;
     const int d1 = (T + K - 1) / K, d2 = (T + 1) / K;
-    const int r1 = d1 * K - T, r2 = (T + 1) - d2 * K;
+    const int tk = T % K;
     const double offset = (SPLAT_DIM != 0 || a.store_quot) ? field_offset(sv.hdr) : 0.0;
 
     // ---- fill -------------------------------------------------------------
+    {
+        // partial sums start at zero (their pad slots stay zero)
+        float4 *z4 = reinterpret_cast<float4 *>(part);
+        const int n4 = (int)((size_t)3 * QS * sizeof(C) / 16);
+        for (int i = tid; i < n4; i += nthr)
+            z4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
     if constexpr (SPLAT_DIM != 0) {
         // zero the line buffers, stage each line's samples with all of the
         // line's threads, then the line's first warp adds them in order
@@ -538,12 +573,19 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
             __syncthreads();
         }
     } else if (LAYOUT == 0) {
+        // zero pads on both sides of every line, then the lines
+        const int back = P - HP - E;
+        for (int q = 0; q < nl; q++) {
+            C *sl = cells + (size_t)q * P;
+            for (int e = tid; e < HP + back; e += nthr)
+                sl[e < HP ? e : HP + E + (e - HP)] = czero<C>();
+        }
         if (a.plain) {
             // single-field lines: the value half only
             const Real *src = reinterpret_cast<const Real *>(a.src_v);
             for (int q = 0; q < nl; q++) {
                 const Real *s_ = src + (line0 + q) * a.L + e0;
-                C *d_ = cells + (size_t)q * P;
+                C *d_ = cells + (size_t)q * P + HP;
                 for (int e = tid; e < E; e += nthr) {
                     C c = czero<C>();
                     c.x = s_[e];
@@ -554,7 +596,7 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
             const C *src = reinterpret_cast<const C *>(a.src_v);
             for (int q = 0; q < nl; q++) {
                 const C *s_ = src + (line0 + q) * a.L + e0;
-                C *d_ = cells + (size_t)q * P;
+                C *d_ = cells + (size_t)q * P + HP;
                 for (int e = tid; e < E; e += nthr)
                     d_[e] = s_[e];
             }
@@ -562,10 +604,20 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
     } else {
         const C *src = reinterpret_cast<const C *>(a.src_v) + gbase;
         const int64_t es = a.elem_stride;
+        {
+            // zero pad rows before and after the lines (two 16-byte vectors a row)
+            uint4 *z = reinterpret_cast<uint4 *>(cells);
+            const int back = P - HP - E;
+            for (int i = tid; i < 2 * (HP + back); i += nthr) {
+                const int r = i >> 1;
+                z[2 * (r < HP ? r : HP + E + (r - HP)) + (i & 1)] = make_uint4(0u, 0u, 0u, 0u);
+            }
+        }
+        C *dcell = cells + (size_t)HP * G;
         if (vec_ok) {
             // two 16-byte vectors per row of G cells
             const int nv = 2 * E;
-            uint4 *d_ = reinterpret_cast<uint4 *>(cells);
+            uint4 *d_ = reinterpret_cast<uint4 *>(dcell);
 #pragma unroll 4
             for (int i = tid; i < nv; i += nthr) {
                 const int row = i >> 1, h = i & 1;
@@ -574,7 +626,7 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
         } else {
             for (int i = tid; i < E * G; i += nthr) {
                 const int row = i / G, gg = i - row * G;
-                cells[i] = gg < nl ? src[row * es + gg] : czero<C>();
+                dcell[i] = gg < nl ? src[row * es + gg] : czero<C>();
             }
         }
     }
@@ -583,14 +635,14 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
     // ---- passes -----------------------------------------------------------
     constexpr bool direct = MODE == 1;
     if (active && !direct) {
-        // partials of the filled data
+        // partials of the filled data (cells past the line are zero pads)
         C o[K];
         const int k0 = j * K;
 #pragma unroll
         for (int i = 0; i < K; i++)
-            o[i] = (k0 + i < E) ? ln[(k0 + i) * ES] : czero<C>();
+            o[i] = ln[(k0 + i) * ES];
         C S, Pr, Su;
-        chunk_partials<C, K, true>(o, k0, E, r1, r2, S, Pr, Su);
+        chunk_partials<C, K>(o, tk, S, Pr, Su);
         pw[0] = S;
         pw[QS] = Pr;
         pw[2 * QS] = Su;
@@ -609,11 +661,9 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
         C S = czero<C>(), Pr = czero<C>(), Su = czero<C>();
         if (active) {
             if (a.scaled)
-                run_pass<Real, C, K, ES, PS, true, direct>(ln, pp0, QS, E, nch, j, T, d1, d2, r1, r2, cs, o, S, Pr,
-                                                           Su);
+                run_pass<Real, C, K, ES, PS, true, direct>(ln, pp0, QS, E, j, T, d1, d2, tk, cs, o, S, Pr, Su);
             else
-                run_pass<Real, C, K, ES, PS, false, direct>(ln, pp0, QS, E, nch, j, T, d1, d2, r1, r2, cu, o, S, Pr,
-                                                            Su);
+                run_pass<Real, C, K, ES, PS, false, direct>(ln, pp0, QS, E, j, T, d1, d2, tk, cu, o, S, Pr, Su);
         }
         __syncthreads();
         if (active) {
@@ -643,7 +693,7 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
     const Real offs = (Real)offset;
     if (LAYOUT == 0) {
         for (int q = 0; q < nl; q++) {
-            const C *c_ = cells + (size_t)q * P;
+            const C *c_ = cells + (size_t)q * P + HP;
             const int64_t gb = (line0 + q) * a.L + e0;
             if (a.store_quot) {
                 if (a.out_f64) {
@@ -671,6 +721,7 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
         }
     } else {
         const int64_t es = a.elem_stride;
+        const C *dcell = cells + (size_t)HP * G;
         if (a.store_quot) {
             // one row of G cells per thread: G quotients, one vector store
             const bool q_vec = G == 4 && vec_ok && (gbase % 4) == 0 && (es % 4) == 0;
@@ -678,7 +729,7 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
                 Real q[G];
 #pragma unroll
                 for (int u = 0; u < G; u++) {
-                    const C c = cells[row * G + u];
+                    const C c = dcell[row * G + u];
                     q[u] = quotient<Real>(c.x, c.y, thr, offs);
                 }
                 const int64_t gi = gbase + row * es;
@@ -707,7 +758,7 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
             C *dst = reinterpret_cast<C *>(a.dst_v) + gbase;
             if (vec_ok) {
                 const int nv = 2 * (s1 - s0);
-                const uint4 *s_ = reinterpret_cast<const uint4 *>(cells + (size_t)s0 * G);
+                const uint4 *s_ = reinterpret_cast<const uint4 *>(dcell + (size_t)s0 * G);
                 for (int i = tid; i < nv; i += nthr) {
                     const int row = s0 + (i >> 1), h = i & 1;
                     *reinterpret_cast<uint4 *>(reinterpret_cast<char *>(dst + row * es) + 16 * h) = s_[i];
@@ -716,15 +767,21 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
                 for (int i = tid; i < (s1 - s0) * G; i += nthr) {
                     const int row = s0 + i / G, gg = i % G;
                     if (gg < nl)
-                        dst[row * es + gg] = cells[row * G + gg];
+                        dst[row * es + gg] = dcell[row * G + gg];
                 }
             }
         }
     }
 }
 
+// Registers per thread: at most 65536 / (512 * AxisMinBlocks) (the
+// compiler's cap for 512-thread CTAs).
+#ifndef FBG_AXIS_MINB
+#define FBG_AXIS_MINB 1
+#endif
+
 template <typename Real, int K, int MODE, int SPLAT_DIM, int LAYOUT>
-__global__ void __launch_bounds__(512, 1) k_axis(const AxisLaunch a, const Geometry g, const SampleView sv)
+__global__ void __launch_bounds__(512, FBG_AXIS_MINB) k_axis(const AxisLaunch a, const Geometry g, const SampleView sv)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int64_t group = blockIdx.x / a.ntiles;
@@ -734,27 +791,39 @@ __global__ void __launch_bounds__(512, 1) k_axis(const AxisLaunch a, const Geome
 // Batched form: the CTAs of one launch take work items (field, block of that
 // field's launch) from a counter until none is left, largest fields first, so
 // fields of uneven size share the GPU without a tail per field.  No CTA waits
-// for another: each item is independent.
-
+// for another: each item is independent.  The item's field description is
+// copied to shared memory, where every thread reads it.
 template <typename Real, int K, int MODE, int SPLAT_DIM, int LAYOUT>
-__global__ void __launch_bounds__(512, 1) k_axis_batch(const BatchAxisField *__restrict__ fields,
-                                                       const BatchItem *__restrict__ items, uint32_t nitems,
-                                                       uint32_t *__restrict__ counter)
+__global__ void __launch_bounds__(512, FBG_AXIS_MINB) k_axis_batch(const BatchAxisField *__restrict__ fields,
+                                                                   const BatchItem *__restrict__ items,
+                                                                   uint32_t nitems, uint32_t *__restrict__ counter)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ uint32_t s_item;
+    __shared__ __align__(16) BatchAxisField s_f;
+    static_assert(sizeof(BatchAxisField) % 4 == 0, "field copy by words");
+    constexpr int kWords = (int)(sizeof(BatchAxisField) / 4);
+    uint32_t last = 0xFFFFFFFFu;
     for (;;) {
         if (threadIdx.x == 0)
             s_item = atomicAdd(counter, 1u);
         __syncthreads();
         const uint32_t it = s_item;
-        __syncthreads();
         if (it >= nitems)
             break;
         const BatchItem bi = items[it];
-        const BatchAxisField &f = fields[bi.field];
-        const int64_t group = bi.block / f.a.ntiles;
-        axis_tile<Real, K, MODE, SPLAT_DIM, LAYOUT>(f.a, f.g, f.sv, group, bi.block - group * f.a.ntiles, smem_raw);
+        if (bi.field != last) {
+            // every thread has passed the barrier above, so no one still reads s_f
+            const uint32_t *src = reinterpret_cast<const uint32_t *>(fields + bi.field);
+            uint32_t *dst = reinterpret_cast<uint32_t *>(&s_f);
+            for (int w = threadIdx.x; w < kWords; w += blockDim.x)
+                dst[w] = src[w];
+            last = bi.field;
+        }
+        __syncthreads();
+        const int64_t group = bi.block / s_f.a.ntiles;
+        axis_tile<Real, K, MODE, SPLAT_DIM, LAYOUT>(s_f.a, s_f.g, s_f.sv, group, bi.block - group * s_f.a.ntiles,
+                                                    smem_raw);
         __syncthreads();
     }
 }

@@ -140,8 +140,11 @@ struct AxisLaunch {
     int64_t ntiles;           // tiles per line
     int halo;                 // extra input cells on each side of a tile
     int extent_max;           // largest shared-memory extent of one line
-    int line_pitch;           // shared-memory cells reserved per line
+    int line_pitch;           // shared-memory cells reserved per line (zero pads included)
+    int line_pad;             // zero cells before cell 0 of a line buffer (T + 1)
     int chunks_pad;           // chunk slots per line (threads per line and field)
+    int part_pitch;           // partial-sum slots per line (zero pads included)
+    int part_pad;             // zero partial slots before chunk 0 (ceil(T / K))
     int passes;               // box passes run in this launch
     int T;
     double alpha;

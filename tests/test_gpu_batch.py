@@ -46,6 +46,18 @@ def uneven_fields(torch, seed=7):
     return fields, host
 
 
+def same(a, b):
+    """Exact equality, NaN positions included; the message says how they differ."""
+    if np.array_equal(a, b, equal_nan=True):
+        return True, ""
+    na, nb = np.isnan(a), np.isnan(b)
+    m = ~na & ~nb
+    d = np.abs(a[m] - b[m])
+    idx = np.argwhere((np.abs(np.nan_to_num(a) - np.nan_to_num(b)) > 0) | (na != nb))
+    return False, (f"{int(np.sum(na != nb))} NaN mismatches, {int(np.sum(d > 0))} differing values, "
+                   f"max diff {float(d.max()) if d.size else 0.0:.3e}, first at {idx[:3].tolist()}")
+
+
 def single(pts, val, s, precision, out_dtype=np.float64):
     return I.barnes(pts, val, s["sigma"], s["x0"], s["step"], s["size"], method=s["method"], num_iter=s["n"],
                     precision=precision, out_dtype=out_dtype)
@@ -62,7 +74,8 @@ def test_batch_equals_single(precision, graph):
         for (pts, val, s), o in zip(host, outs):
             ref = single(pts, val, s, precision)
             assert o.shape == ref.shape
-            assert np.array_equal(o, ref, equal_nan=True), (s, rep)
+            ok, msg = same(o, ref)
+            assert ok, (s, rep, msg)
     plan.close()
 
 
@@ -80,7 +93,8 @@ def test_batch_refill_inputs():
         host[k] = (pts, nv, s)
     outs = [o.cpu().numpy() for o in plan.run()]
     for (pts, val, s), o in zip(host, outs):
-        assert np.array_equal(o, single(pts, val, s, "fp32c"), equal_nan=True)
+        ok, msg = same(o, single(pts, val, s, "fp32c"))
+        assert ok, (s, msg)
     plan.close()
 
 
