@@ -8,7 +8,7 @@ num_iter = 4, max_dist = 3.5; float32-compensated form (fp32c).  Seeded
 synthetic data stand in for observations.
 
 Metric: Mgridpts/s = batch grid points x steps / time.  One step is one run
-of a batch plan (fb_batch_run: one sample sort and one persistent launch per
+of a batch plan (fb_batch_run: one sample sort and one launch per
 axis for all B fields, replayed from a CUDA graph).  `value` has the inputs
 resident in HBM; `e2e` runs the C-ABI host-buffer form (fb_batch_run_host)
 from pinned host buffers, copies of every field's samples in and results out
@@ -142,7 +142,7 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def cpu_oracle_rate(nthreads, seconds=12.0, max_fields=3):
+def cpu_oracle_rate(nthreads, seconds=12.0, max_fields=60):
     """The reference's algorithm (the C oracle) on this host: Mgridpts/s."""
     from oracle import oracle
     oracle.build()
@@ -327,7 +327,7 @@ def main():
     if args.quick:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": "Mgridpts/s", "quick": True,
-                              "knobs": knobs, "ms_per_step": t_ms / args.steps,
+                              "knobs": knobs, "ms_per_step": t_ms / args.steps, "clocks": clk.summary(),
                               "stage_ms": {names[k]: v for k, v in stage_ms.items()},
                               "single_call_value": single_value,
                               "single_call_stage_ms_per_field": {k: v for k, v in single_stage_ms.items()}}),

@@ -33,7 +33,11 @@ static bool direct_mode(int precision, int T) { return T <= (precision == 0 ? Di
 // short chunk; a plan may pin 17 or 33 for float32 sliding sums.
 static int kchunk_of(int precision, int T, int kchunk)
 {
-    if (precision == 0 || direct_mode(precision, T) || T <= 32)
+    if (direct_mode(precision, T))
+        return K64;
+    if (precision == 0)
+        return 2 * T + 1 >= K64 ? K64 : K9;
+    if (T <= 32)
         return K64;
     if (kchunk == K64 || kchunk == K32)
         return kchunk;
@@ -61,28 +65,32 @@ size_t axis_smem_limit()
 
 static int even(int64_t x) { return (int)((x + 1) / 2 * 2); }
 
-// Shared-memory geometry of a launch whose longest line extent is E: chunk
-// slots, the line buffer with T + 1 zero cells before the line and zeros up
-// to T + 1 cells past the last chunk, and the partial-sum arrays with zero
-// slots for the ceil(T/K) chunks before and floor((T+1)/K) + 1 after.
+// Shared-memory geometry of a launch whose longest line extent is E.  Chunk
+// slots: ceil(E/K) for direct sums, ceil((E + T + 1)/K) for sliding passes
+// (their chunks alternate between two grids T + 1 cells apart; a chunk that
+// lies wholly outside [0, E) in a pass reads clamped cells and is cleared).
+// Every read lies in [-(T + 1 + K), E + T + K): the line buffer has
+// T + 1 + K zero cells before the line and T + K after it.  The two partial-sum arrays (S, X) have q + 1
+// zero slots on both sides, q = floor((2T + 1)/K).
 static void set_geometry(int precision, AxisLaunch &a, int K, int64_t E)
 {
-    const int nch = (int)((E + K - 1) / K);
+    const bool direct = direct_mode(precision, a.T);
+    const int nact = (int)(direct ? (E + K - 1) / K : (E + a.T + 1 + K - 1) / K);
     const int unit = a.layout == 0 ? 32 : 32 / col_g(precision);
-    a.chunks_pad = (nch + unit - 1) / unit * unit;
+    a.chunks_pad = (nact + unit - 1) / unit * unit;
     a.extent_max = (int)E;
-    a.line_pad = a.T + 1;
-    a.line_pitch = even((int64_t)nch * K + 2 * (int64_t)a.line_pad);
-    const int d1 = (a.T + K - 1) / K, d2 = (a.T + 1) / K;
-    a.part_pad = d1;
-    a.part_pitch = even((int64_t)d1 + a.chunks_pad + d2 + 1);
+    a.line_pad = a.T + 1 + K;
+    a.line_pitch = even((int64_t)a.line_pad + E + a.T + K);
+    const int q = (2 * a.T + 1) / K;
+    a.part_pad = q + 1;
+    a.part_pitch = even((int64_t)a.part_pad + a.chunks_pad + q + 2);
 }
 
 size_t axis_smem_bytes(int precision, const AxisLaunch &a)
 {
     const size_t cs = cell_size(precision);
     const size_t nlc = a.layout == 0 ? (size_t)a.lines_per_cta : (size_t)col_g(precision);
-    size_t b = nlc * ((size_t)a.line_pitch + 3 * (size_t)a.part_pitch) * cs;
+    size_t b = nlc * ((size_t)a.line_pitch + 2 * (size_t)a.part_pitch) * cs;
     if (a.fill_splat)
         b += nlc * kStage * (precision == 0 ? sizeof(StageRec<double>) : sizeof(StageRec<float>));
     return b;
@@ -151,26 +159,29 @@ bool axis_shape(int precision, AxisLaunch &a)
 
 cudaError_t launch_axis_f32(int k, int mode, int sd, const AxisLaunch &a, const Geometry &g, const SampleView &sv,
                             cudaStream_t st);
-cudaError_t launch_axis_f64(int mode, int sd, const AxisLaunch &a, const Geometry &g, const SampleView &sv,
+cudaError_t launch_axis_f64(int k, int mode, int sd, const AxisLaunch &a, const Geometry &g, const SampleView &sv,
                             cudaStream_t st);
 
-cudaError_t launch_axis_batch_f32(int op, int k, int mode, int sd, int layout, const BatchAxisField *fields,
-                                  const BatchItem *items, uint32_t nitems, uint32_t *counter, size_t smem,
-                                  int threads, int *grid, cudaStream_t st);
-cudaError_t launch_axis_batch_f64(int op, int mode, int sd, int layout, const BatchAxisField *fields,
-                                  const BatchItem *items, uint32_t nitems, uint32_t *counter, size_t smem,
-                                  int threads, int *grid, cudaStream_t st);
+cudaError_t launch_axis_batch_f32(int op, int k, int mode, int sd, const AxisLaunch &a, const Geometry &g,
+                                  const SampleView &sv, const TilePtrs *fields, uint32_t bpf, uint32_t nitems,
+                                  int *grid, cudaStream_t st);
+cudaError_t launch_axis_batch_f64(int op, int k, int mode, int sd, const AxisLaunch &a, const Geometry &g,
+                                  const SampleView &sv, const TilePtrs *fields, uint32_t bpf, uint32_t nitems,
+                                  int *grid, cudaStream_t st);
 
-int axis_kernel_k(int precision, const AxisLaunch &a) { return kchunk_of(precision, a.T, a.kchunk); }
-int axis_kernel_mode(int precision, int T) { return direct_mode(precision, T) ? 1 : 0; }
 
-cudaError_t launch_axis_batch(int op, int precision, int k, int mode, int sd, int layout,
-                              const BatchAxisField *fields, const BatchItem *items, uint32_t nitems,
-                              uint32_t *counter, size_t smem, int threads, int *grid, cudaStream_t st)
+cudaError_t launch_axis_batch(int op, int precision, const AxisLaunch &a, const Geometry &g, const SampleView &sv,
+                              const TilePtrs *fields, uint32_t bpf, uint32_t nitems, int *grid, cudaStream_t st)
 {
+    const int sd = a.fill_splat ? g.dim : 0;
+    if (a.layout == 1 && a.fill_splat)
+        return cudaErrorInvalidValue;
+    const int mode = direct_mode(precision, a.T) ? 1 : 0;
     if (precision == 0)
-        return launch_axis_batch_f64(op, mode, sd, layout, fields, items, nitems, counter, smem, threads, grid, st);
-    return launch_axis_batch_f32(op, k, mode, sd, layout, fields, items, nitems, counter, smem, threads, grid, st);
+        return launch_axis_batch_f64(op, kchunk_of(precision, a.T, a.kchunk), mode, sd, a, g, sv, fields, bpf,
+                                     nitems, grid, st);
+    return launch_axis_batch_f32(op, kchunk_of(precision, a.T, a.kchunk), mode, sd, a, g, sv, fields, bpf, nitems,
+                                 grid, st);
 }
 
 cudaError_t launch_axis(int precision, const AxisLaunch &a, const Geometry &g, const SampleView &sv,
@@ -181,7 +192,7 @@ cudaError_t launch_axis(int precision, const AxisLaunch &a, const Geometry &g, c
         return cudaErrorInvalidValue;
     const int mode = direct_mode(precision, a.T) ? 1 : 0;
     if (precision == 0)
-        return launch_axis_f64(mode, sd, a, g, sv, st);
+        return launch_axis_f64(kchunk_of(precision, a.T, a.kchunk), mode, sd, a, g, sv, st);
     return launch_axis_f32(kchunk_of(precision, a.T, a.kchunk), mode, sd, a, g, sv, st);
 }
 

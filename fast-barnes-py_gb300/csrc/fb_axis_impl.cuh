@@ -99,6 +99,15 @@ __device__ __forceinline__ float2 csplat<float2>(double x) { return make_float2(
 template <>
 __device__ __forceinline__ double2 csplat<double2>(double x) { return make_double2(x, x); }
 
+// 16-byte asynchronous global -> shared copies (no registers held while the
+// data is in flight, so a thread can have all of its copies outstanding)
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // ---------------------------------------------------------------------------
 // one line seen by one thread: cell e lives at s[e * ES]; the line buffer has
 // zero cells on both sides (T + 1 before the line, up to the end of the last
@@ -117,38 +126,90 @@ struct PassCoef {
     }
 };
 
-// Slides the window over the chunk [k0, k0 + K): forward from A0 (window at
-// k0) over the first half, backward from A1 (window at k0 + K) over the rest;
-// the two halves are independent, so their steps are interleaved.
+// Sliding passes move every thread's chunk by T + 1 cells, alternately to the
+// left and back to the right, so that the window cells on one side of the new
+// chunk are exactly the thread's own previous chunk, still in registers: a
+// pass reads one cell per output from shared memory (the other side of the
+// window) instead of two.  F grid: chunk j = [jK, jK + K); A grid: chunk j =
+// [jK - T - 1, jK - T - 1 + K).  Even passes go F -> A ("left"), odd passes
+// A -> F ("right").  Needs 2T + 1 >= K.
+//
+// Window sums (anchors) come from the previous pass's per-chunk sums S and
+// one partial sum X of r = (2T + 1) mod K cells (the last r cells of an F
+// chunk, the first r of an A chunk): whole pieces inside the window, nothing
+// subtracted.  The thread slides forward from the anchor at its chunk start
+// over the first half and backward from the one at its chunk end over the
+// rest; the two halves are independent, so their steps are interleaved.
+//
+// Left pass: own previous chunk P = F chunk j at b = jK, outputs at
+// a = b - T - 1; s[m] = cell b - 2T - 2 + m.  Output i: window
+// [b + i - 2T - 1, b + i - 1], tails s[i] and P[i].
+// A chunk wholly left of the line (a + K <= 0) would read below the buffer's
+// zero cells; its reads are moved up to the buffer start (lo), and its
+// outputs are cleared afterwards anyway.
 template <typename C, int K, int ES, bool SCALED>
-__device__ __forceinline__ void slide(const C *__restrict__ s, int k0, int T, C A0, C A1,
-                                      const PassCoef<C, SCALED> &c, C (&o)[K])
+__device__ __forceinline__ void pass_left(const C *__restrict__ ln, int b, int T, int lo, C A0, C A1,
+                                          const PassCoef<C, SCALED> &c, C (&o)[K])
 {
-    constexpr int H = K / 2;   // forward steps 0 .. H-1, backward steps K-1 .. H
-    C af = A0, ab = A1;
-    const C *lo = s + (k0 - T - 1) * ES;   // cell k0 - T - 1
-    const C *hi = s + (k0 + T + 1) * ES;   // cell k0 + T + 1
-    C prev = lo[0];
-    C odb = lo[K * ES];                    // cell k0 + K - 1 - T
+    constexpr int H = K / 2;
+    const C *s = ln + max(b - 2 * T - 2, lo) * ES;
+    C af = A0, ab = A1;          // windows at a and a + K
+    C prev = s[0];
+    C nb = s[K * ES];
 #pragma unroll
     for (int i = 0; i < H; i++) {
-        const C nwf = hi[i * ES];                   // k0 + i + T + 1
-        const C odf = lo[(i + 1) * ES];             // k0 + i - T
-        const C nwb = hi[(K - 1 - i) * ES];         // kb + T + 1, kb = k0 + K - 1 - i
-        const C tlb = lo[(K - 1 - i) * ES];         // kb - T - 1
-        o[i] = c.out(af, cadd(prev, nwf));
-        af = csub(cadd(af, nwf), odf);
-        prev = odf;
-        ab = cadd(csub(ab, nwb), odb);
-        o[K - 1 - i] = c.out(ab, cadd(tlb, nwb));
-        odb = tlb;
+        // forward: output i, then the window moves to i + 1 (+P[i], -s[i+1])
+        const C x = s[(i + 1) * ES];
+        const C pf = o[i];
+        o[i] = c.out(af, cadd(prev, pf));
+        af = cadd(af, csub(pf, x));
+        prev = x;
+        // backward: the window moves to k (+s[k+1], -P[k]), then output k
+        const int k = K - 1 - i;
+        const C y = s[k * ES];
+        const C pk = o[k];
+        ab = cadd(ab, csub(nb, pk));
+        o[k] = c.out(ab, cadd(y, pk));
+        nb = y;
     }
     {
-        const C nwb = hi[H * ES];
-        const C tlb = lo[H * ES];
-        ab = cadd(csub(ab, nwb), odb);
-        o[H] = c.out(ab, cadd(tlb, nwb));
+        const C y = s[H * ES];
+        const C pk = o[H];
+        ab = cadd(ab, csub(nb, pk));
+        o[H] = c.out(ab, cadd(y, pk));
     }
+}
+
+// Right pass: own previous chunk P = A chunk j at b = jK - T - 1, outputs at
+// a = b + T + 1 = jK; s[m] = cell b + 2T + 2 + m.  Output i: window
+// [b + i + 1, b + i + 2T + 1], tails P[i] and s[i].  A0 is the window at a,
+// A1 the one at a + K - 1.
+// A chunk wholly right of the line (a >= E) reads as if it started at E - 1
+// (inside the buffer's zero cells); its outputs are cleared afterwards.
+template <typename C, int K, int ES, bool SCALED>
+__device__ __forceinline__ void pass_right(const C *__restrict__ ln, int b, int T, int E, C A0, C A1,
+                                           const PassCoef<C, SCALED> &c, C (&o)[K])
+{
+    constexpr int H = K / 2;
+    const C *s = ln + (min(b + T + 1, E - 1) + T + 1) * ES;
+    C af = A0, ab = A1;
+    C hi = s[(K - 1) * ES];
+#pragma unroll
+    for (int i = 0; i < H; i++) {
+        // forward: output i, then the window moves to i + 1 (+s[i], -P[i+1])
+        const C x = s[i * ES];
+        const C pf = o[i];
+        o[i] = c.out(af, cadd(pf, x));
+        af = cadd(af, csub(x, o[i + 1]));
+        // backward: output k, then the window moves to k - 1 (+P[k], -s[k-1])
+        const int k = K - 1 - i;
+        const C pk = o[k];
+        o[k] = c.out(ab, cadd(pk, hi));
+        const C lo = s[(k - 1) * ES];
+        ab = cadd(ab, csub(pk, lo));
+        hi = lo;
+    }
+    o[H] = c.out(ab, cadd(o[H], hi));
 }
 
 // Narrow kernels (T <= DirectMax): every output is summed directly from the
@@ -197,101 +258,57 @@ __device__ __forceinline__ void direct_dispatch(int T, const C *s, int k0, const
     }
 }
 
-// Sums of a chunk that the next pass's anchors are built from: the whole
-// chunk (S), its first R2 cells (Pre) and its cells from R1 on (Suf), as sums
-// of the (at most three) segments that R1 and R2 cut the chunk into.
-template <typename C, int K, int R1, int R2>
-__device__ __forceinline__ void partials_fixed(const C (&o)[K], C &S, C &Pre, C &Suf)
+// The sums a chunk leaves for the next pass: S = o[0] + S1 with S1 the sum
+// of o[1..K-1], and X = the first R cells (PRE) or the last R cells (suffix),
+// each accumulated once over disjoint segments.
+template <typename C, int K, int R, bool PRE>
+__device__ __forceinline__ void chunk_sums_fixed(const C (&o)[K], C &S, C &S1, C &X)
 {
-    constexpr int B0 = R1 < R2 ? R1 : R2, B1 = R1 < R2 ? R2 : R1;
-    C s0 = czero<C>(), s1 = czero<C>(), s2 = czero<C>();
+    constexpr int B = PRE ? (R > 0 ? R : 1) : (K - R > 1 ? K - R : 1);   // segment split inside [1, K)
+    C a = czero<C>(), z = czero<C>();
 #pragma unroll
-    for (int i = 0; i < B0; i++)
-        s0 = cadd(s0, o[i]);
+    for (int i = 1; i < B; i++)
+        a = cadd(a, o[i]);
 #pragma unroll
-    for (int i = B0; i < B1; i++)
-        s1 = cadd(s1, o[i]);
-#pragma unroll
-    for (int i = B1; i < K; i++)
-        s2 = cadd(s2, o[i]);
-    S = cadd(cadd(s0, s1), s2);
-    if (R2 <= R1) {
-        Pre = s0;   // [0, R2)
-        Suf = s2;   // [R1, K)
-    } else {
-        Pre = cadd(s0, s1);   // [0, R1) + [R1, R2)
-        Suf = cadd(s1, s2);   // [R1, R2) + [R2, K)
-    }
+    for (int i = B; i < K; i++)
+        z = cadd(z, o[i]);
+    S1 = cadd(a, z);
+    S = cadd(o[0], S1);
+    if (PRE)
+        X = R == 0 ? czero<C>() : cadd(o[0], a);       // o[0] + o[1..R-1]
+    else
+        X = R == 0 ? czero<C>() : (R == K ? S : z);    // o[K-R..K-1]
 }
 
-// t = T mod K selects R1 = (K - t) mod K, R2 = (t + 1) mod K at compile time
-// (one indirect branch per pass, the same for every thread).
-template <typename C, int K>
-__device__ __forceinline__ void chunk_partials(const C (&o)[K], int t, C &S, C &Pre, C &Suf)
+template <typename C, int K, bool PRE>
+__device__ __forceinline__ void chunk_sums(const C (&o)[K], int r, C &S, C &S1, C &X)
 {
-#define FBG_PC(TT)                                                                                                  \
-    case TT:                                                                                                        \
-        if constexpr (TT < K)                                                                                       \
-            partials_fixed<C, K, (K - TT) % K, (TT + 1) % K>(o, S, Pre, Suf);                                       \
+#define FBG_CS(RR)                                                                                                  \
+    case RR:                                                                                                        \
+        if constexpr (RR < K)                                                                                       \
+            chunk_sums_fixed<C, K, RR, PRE>(o, S, S1, X);                                                           \
         break;
-    switch (t) {
-        FBG_PC(0) FBG_PC(1) FBG_PC(2) FBG_PC(3) FBG_PC(4) FBG_PC(5) FBG_PC(6) FBG_PC(7) FBG_PC(8) FBG_PC(9)
-        FBG_PC(10) FBG_PC(11) FBG_PC(12) FBG_PC(13) FBG_PC(14) FBG_PC(15) FBG_PC(16) FBG_PC(17) FBG_PC(18)
-        FBG_PC(19) FBG_PC(20) FBG_PC(21) FBG_PC(22) FBG_PC(23) FBG_PC(24) FBG_PC(25) FBG_PC(26) FBG_PC(27)
-        FBG_PC(28) FBG_PC(29) FBG_PC(30) FBG_PC(31) FBG_PC(32)
+    switch (r) {
+        FBG_CS(0) FBG_CS(1) FBG_CS(2) FBG_CS(3) FBG_CS(4) FBG_CS(5) FBG_CS(6) FBG_CS(7) FBG_CS(8) FBG_CS(9)
+        FBG_CS(10) FBG_CS(11) FBG_CS(12) FBG_CS(13) FBG_CS(14) FBG_CS(15) FBG_CS(16) FBG_CS(17) FBG_CS(18)
+        FBG_CS(19) FBG_CS(20) FBG_CS(21) FBG_CS(22) FBG_CS(23) FBG_CS(24) FBG_CS(25) FBG_CS(26) FBG_CS(27)
+        FBG_CS(28) FBG_CS(29) FBG_CS(30) FBG_CS(31) FBG_CS(32)
     default: break;
     }
-#undef FBG_PC
+#undef FBG_CS
 }
-static_assert(K32 <= 33 && K64 <= 33, "chunk_partials lists t up to 32");
+static_assert(K32 <= 33 && K64 <= 33, "chunk_sums lists r up to 32");
 
-// Window sums at k0 = jK and k0 + K from the chunk partials (T >= 1):
-// window [k0-T, k0+T] = Suf[m1] + S[m1+1 .. m2-1] + Pre[m2], m1 = j - d1,
-// m2 = j + d2 (d1 = ceil(T/K), d2 = floor((T+1)/K)).  Every term is a sum of
-// cells inside the window: nothing is subtracted.  The partial arrays have
-// zero slots for the chunks before and after the line.
-template <int PS, typename C>
-__device__ __forceinline__ void anchors(const C *__restrict__ S, const C *__restrict__ Pre, const C *__restrict__ Suf,
-                                        int j, int d1, int d2, C &A0, C &A1)
-{
-    const int m1 = j - d1, m2 = j + d2;
-    C mid = czero<C>();
-    for (int m = m1 + 2; m <= m2 - 1; m++)
-        mid = cadd(mid, S[m * PS]);
-    const bool two = (m2 - m1) >= 2;
-    A0 = cadd(cadd(cadd(Suf[m1 * PS], two ? S[(m1 + 1) * PS] : czero<C>()), mid), Pre[m2 * PS]);
-    A1 = cadd(cadd(cadd(Suf[(m1 + 1) * PS], mid), two ? S[m2 * PS] : czero<C>()), Pre[(m2 + 1) * PS]);
-}
-
-// Outputs of the chunk at or beyond the line extent are not part of the line:
-// zero them so that the partial sums see the line's zeros there.
+// Outputs outside the line [0, E) are zero (the line's own zeros).
 template <typename C, int K>
-__device__ __forceinline__ void clip_tail(C (&o)[K], int k0, int E)
+__device__ __forceinline__ void clip_chunk(C (&o)[K], int a, int E)
 {
-    if (k0 + K > E) {
+    if (a < 0 || a + K > E) {
 #pragma unroll
         for (int i = 0; i < K; i++)
-            if (k0 + i >= E)
+            if (a + i < 0 || a + i >= E)
                 o[i] = czero<C>();
     }
-}
-
-// One box pass of one thread's chunk: outputs into o, next partials into S/P/U.
-template <typename Real, typename C, int K, int ES, int PS, bool SCALED, bool DIRECT>
-__device__ __forceinline__ void run_pass(const C *__restrict__ ln, const C *__restrict__ pp, int QS, int E, int j,
-                                         int T, int d1, int d2, int tk, const PassCoef<C, SCALED> &c, C (&o)[K],
-                                         C &S, C &P, C &U)
-{
-    const int k0 = j * K;
-    if constexpr (DIRECT) {
-        direct_dispatch<Real, C, K, ES, 0, SCALED>(T, ln, k0, c, o);
-        return;
-    }
-    C A0, A1;
-    anchors<PS>(pp, pp + QS, pp + 2 * QS, j, d1, d2, A0, A1);
-    slide<C, K, ES, SCALED>(ln, k0, T, A0, A1, c, o);
-    clip_tail(o, k0, E);
-    chunk_partials<C, K>(o, tk, S, P, U);
 }
 
 // NaN where the weight is below the mask level, else vg / wg + offset
@@ -325,7 +342,7 @@ struct LineRanges {
 
 template <int DIM>
 __device__ __forceinline__ LineRanges line_ranges(int64_t line, int64_t e0, int E, const Geometry &g,
-                                                  const SampleView &sv)
+                                                  const SampleView &sv, const uint32_t *__restrict__ bin_start)
 {
     LineRanges r;
     r.n = 0;
@@ -336,15 +353,15 @@ __device__ __forceinline__ LineRanges line_ranges(int64_t line, int64_t e0, int 
         if (b1 > (int64_t)sv.nbins - 1)
             b1 = (int64_t)sv.nbins - 1;
         if (b0 <= b1) {
-            r.b[0] = sv.bin_start[b0];
-            r.e[0] = sv.bin_start[b1 + 1];
+            r.b[0] = bin_start[b0];
+            r.e[0] = bin_start[b1 + 1];
             r.n = 1;
         }
     } else if (DIM == 2) {
         // samples whose lower corner row is line - 1 or line, in that order
         const int64_t b0 = line >= 1 ? line - 1 : line;
-        r.b[0] = sv.bin_start[b0];
-        r.e[0] = sv.bin_start[line + 1];
+        r.b[0] = bin_start[b0];
+        r.e[0] = bin_start[line + 1];
         r.n = 1;
     } else {
         const int64_t H = g.size[1];
@@ -354,8 +371,8 @@ __device__ __forceinline__ LineRanges line_ranges(int64_t line, int64_t e0, int 
                 continue;
             const int64_t rb = (z - dz) * H;
             const int64_t b0 = y >= 1 ? rb + y - 1 : rb + y;
-            r.b[r.n] = sv.bin_start[b0];
-            r.e[r.n] = sv.bin_start[rb + y + 1];
+            r.b[r.n] = bin_start[b0];
+            r.e[r.n] = bin_start[rb + y + 1];
             r.n++;
         }
     }
@@ -459,8 +476,8 @@ struct ColG {
 // MODE: 0 = sliding windows, 1 = direct sums (narrow kernels).
 // One tile of one launch: line group `group`, tile `tile` along the lines.
 template <typename Real, int K, int MODE, int SPLAT_DIM, int LAYOUT>
-__device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g, const SampleView &sv, int64_t group,
-                                          int64_t tile, unsigned char *smem_raw)
+__device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g, const SampleView &sv,
+                                          const TilePtrs &fp, int64_t group, int64_t tile, unsigned char *smem_raw)
 {
     using C = typename CellOf<Real>::T;
     constexpr int G = LAYOUT == 0 ? 1 : ColG<C>::G;
@@ -518,17 +535,18 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
         pp0 = part + (size_t)PF * G + li;
     }
     C *pw = const_cast<C *>(pp0) + (size_t)j * PS;   // this chunk's S slot
-    const bool active = li < nl && j < nch;
     const int T = a.T;
-    const int d1 = (T + K - 1) / K, d2 = (T + 1) / K;
-    const int tk = T % K;
-    const double offset = (SPLAT_DIM != 0 || a.store_quot) ? field_offset(sv.hdr) : 0.0;
+    // sliding passes need the chunks of both grids that touch [0, E)
+    const int nact = MODE == 1 ? nch : (E + T + 1 + K - 1) / K;
+    const bool active = li < nl && j < nact;
+    const int q = (2 * T + 1) / K, r = (2 * T + 1) - q * K;
+    const double offset = (SPLAT_DIM != 0 || a.store_quot) ? field_offset(fp.hdr) : 0.0;
 
     // ---- fill -------------------------------------------------------------
     {
         // partial sums start at zero (their pad slots stay zero)
         float4 *z4 = reinterpret_cast<float4 *>(part);
-        const int n4 = (int)((size_t)3 * QS * sizeof(C) / 16);
+        const int n4 = (int)((size_t)2 * QS * sizeof(C) / 16);
         for (int i = tid; i < n4; i += nthr)
             z4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
@@ -539,7 +557,7 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
         const int n4 = (int)((size_t)NLC * P * sizeof(C) / 16);
         for (int i = tid; i < n4; i += nthr)
             z4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        StageRec<Real> *stage = reinterpret_cast<StageRec<Real> *>(part + (size_t)3 * QS);
+        StageRec<Real> *stage = reinterpret_cast<StageRec<Real> *>(part + (size_t)2 * QS);
         const SampleRec<Real> *recs = reinterpret_cast<const SampleRec<Real> *>(sv.rec);
         __shared__ uint32_t s_rounds;
         if (tid == 0)
@@ -548,7 +566,7 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
         rg.n = 0;
         uint32_t total = 0;
         if (li < nl) {
-            rg = line_ranges<SPLAT_DIM>(line0 + li, e0, E, g, sv);
+            rg = line_ranges<SPLAT_DIM>(line0 + li, e0, E, g, sv, fp.bin_start);
             total = range_total(rg);
         }
         __syncthreads();
@@ -563,7 +581,7 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
                 for (int q = j; q < kStage; q += CP) {
                     const uint32_t pos = base + q;
                     if (pos < total)
-                        my_stage[q] = make_stage<SPLAT_DIM, Real>(recs[sv.sorted_idx[range_at(rg, pos)]], line0 + li,
+                        my_stage[q] = make_stage<SPLAT_DIM, Real>(recs[range_at(rg, pos)], line0 + li,
                                                                   g, offset);
                 }
             }
@@ -582,7 +600,7 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
         }
         if (a.plain) {
             // single-field lines: the value half only
-            const Real *src = reinterpret_cast<const Real *>(a.src_v);
+            const Real *src = reinterpret_cast<const Real *>(fp.src);
             for (int q = 0; q < nl; q++) {
                 const Real *s_ = src + (line0 + q) * a.L + e0;
                 C *d_ = cells + (size_t)q * P + HP;
@@ -593,7 +611,7 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
                 }
             }
         } else {
-            const C *src = reinterpret_cast<const C *>(a.src_v);
+            const C *src = reinterpret_cast<const C *>(fp.src);
             for (int q = 0; q < nl; q++) {
                 const C *s_ = src + (line0 + q) * a.L + e0;
                 C *d_ = cells + (size_t)q * P + HP;
@@ -602,7 +620,7 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
             }
         }
     } else {
-        const C *src = reinterpret_cast<const C *>(a.src_v) + gbase;
+        const C *src = reinterpret_cast<const C *>(fp.src) + gbase;
         const int64_t es = a.elem_stride;
         {
             // zero pad rows before and after the lines (two 16-byte vectors a row)
@@ -615,14 +633,14 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
         }
         C *dcell = cells + (size_t)HP * G;
         if (vec_ok) {
-            // two 16-byte vectors per row of G cells
+            // two 16-byte asynchronous copies per row of G cells
             const int nv = 2 * E;
             uint4 *d_ = reinterpret_cast<uint4 *>(dcell);
-#pragma unroll 4
             for (int i = tid; i < nv; i += nthr) {
                 const int row = i >> 1, h = i & 1;
-                d_[i] = *reinterpret_cast<const uint4 *>(reinterpret_cast<const char *>(src + row * es) + 16 * h);
+                cp_async16(d_ + i, reinterpret_cast<const char *>(src + row * es) + 16 * h);
             }
+            cp_async_wait_all();
         } else {
             for (int i = tid; i < E * G; i += nthr) {
                 const int row = i / G, gg = i - row * G;
@@ -633,21 +651,6 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
     __syncthreads();
 
     // ---- passes -----------------------------------------------------------
-    constexpr bool direct = MODE == 1;
-    if (active && !direct) {
-        // partials of the filled data (cells past the line are zero pads)
-        C o[K];
-        const int k0 = j * K;
-#pragma unroll
-        for (int i = 0; i < K; i++)
-            o[i] = ln[(k0 + i) * ES];
-        C S, Pr, Su;
-        chunk_partials<C, K>(o, tk, S, Pr, Su);
-        pw[0] = S;
-        pw[QS] = Pr;
-        pw[2 * QS] = Su;
-    }
-
     PassCoef<C, false> cu;
     cu.alpha = csplat<C>(a.alpha);
     cu.inv = csplat<C>(1.0);
@@ -655,33 +658,105 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
     cs.alpha = csplat<C>(a.alpha * a.inv_norm);
     cs.inv = csplat<C>(a.inv_norm);
 
-    for (int pass = 0; pass < a.passes; pass++) {
-        __syncthreads();
-        C o[K];
-        C S = czero<C>(), Pr = czero<C>(), Su = czero<C>();
-        if (active) {
-            if (a.scaled)
-                run_pass<Real, C, K, ES, PS, true, direct>(ln, pp0, QS, E, j, T, d1, d2, tk, cs, o, S, Pr, Su);
-            else
-                run_pass<Real, C, K, ES, PS, false, direct>(ln, pp0, QS, E, j, T, d1, d2, tk, cu, o, S, Pr, Su);
-        }
-        __syncthreads();
-        if (active) {
+    if constexpr (MODE == 1) {
+        // direct sums, F grid every pass
+        for (int pass = 0; pass < a.passes; pass++) {
+            __syncthreads();
+            C o[K];
             const int k0 = j * K;
-            if (k0 + K <= E) {
-#pragma unroll
-                for (int i = 0; i < K; i++)
-                    ln[(k0 + i) * ES] = o[i];
-            } else {
-#pragma unroll
-                for (int i = 0; i < K; i++)
-                    if (k0 + i < E)
-                        ln[(k0 + i) * ES] = o[i];
+            if (active) {
+                if (a.scaled)
+                    direct_dispatch<Real, C, K, ES, 0, true>(T, ln, k0, cs, o);
+                else
+                    direct_dispatch<Real, C, K, ES, 0, false>(T, ln, k0, cu, o);
             }
-            if (!direct) {
-                pw[0] = S;
-                pw[QS] = Pr;
-                pw[2 * QS] = Su;
+            __syncthreads();
+            if (active) {
+                if (k0 + K <= E) {
+#pragma unroll
+                    for (int i = 0; i < K; i++)
+                        ln[(k0 + i) * ES] = o[i];
+                } else {
+#pragma unroll
+                    for (int i = 0; i < K; i++)
+                        if (k0 + i < E)
+                            ln[(k0 + i) * ES] = o[i];
+                }
+            }
+        }
+    } else {
+        // the thread's chunk lives in o[] from pass to pass
+        C o[K];
+        C own_s = czero<C>(), own_s1 = czero<C>();
+        if (active) {
+            const int b = j * K;   // F chunk of the filled line (zero cells past E)
+#pragma unroll
+            for (int i = 0; i < K; i++)
+                o[i] = ln[(b + i) * ES];
+            C X;
+            chunk_sums<C, K, false>(o, r, own_s, own_s1, X);
+            pw[0] = own_s;
+            pw[QS] = X;
+        }
+        const C *pS = pp0;
+        const C *pX = pp0 + QS;
+        for (int pass = 0; pass < a.passes; pass++) {
+            __syncthreads();
+            const bool left = (pass & 1) == 0;
+            const bool more = pass + 1 < a.passes;
+            const int a0 = left ? j * K - T - 1 : j * K;   // this pass's chunk
+            C X = czero<C>();
+            if (active) {
+                C mid = czero<C>();
+                if (left) {
+                    for (int m = 1; m < q; m++)
+                        mid = cadd(mid, pS[(j - m) * PS]);
+                    const C A0 = cadd(cadd(pX[(j - q - 1) * PS], pS[(j - q) * PS]), mid);
+                    const C A1 = cadd(cadd(pX[(j - q) * PS], mid), own_s);
+                    const int b = j * K;
+                    if (a.scaled)
+                        pass_left<C, K, ES, true>(ln, b, T, -HP, A0, A1, cs, o);
+                    else
+                        pass_left<C, K, ES, false>(ln, b, T, -HP, A0, A1, cu, o);
+                } else {
+                    for (int m = 1; m < q; m++)
+                        mid = cadd(mid, pS[(j + m) * PS]);
+                    const int b = j * K - T - 1;
+                    // cell b + qK + r = jK + T (moved inside the buffer for a
+                    // chunk wholly right of the line, like its other reads)
+                    const C A0 = cadd(cadd(cadd(own_s1, mid), pX[(j + q) * PS]), ln[(min(j * K, E - 1) + T) * ES]);
+                    const C A1 = cadd(cadd(mid, pS[(j + q) * PS]), pX[(j + q + 1) * PS]);
+                    if (a.scaled)
+                        pass_right<C, K, ES, true>(ln, b, T, E, A0, A1, cs, o);
+                    else
+                        pass_right<C, K, ES, false>(ln, b, T, E, A0, A1, cu, o);
+                }
+                clip_chunk(o, a0, E);
+                if (more) {
+                    // the next pass goes the other way: it needs the first r
+                    // cells of an A chunk, the last r of an F chunk
+                    if (left)
+                        chunk_sums<C, K, true>(o, r, own_s, own_s1, X);
+                    else
+                        chunk_sums<C, K, false>(o, r, own_s, own_s1, X);
+                }
+            }
+            __syncthreads();
+            if (active) {
+                if (a0 >= 0 && a0 + K <= E) {
+#pragma unroll
+                    for (int i = 0; i < K; i++)
+                        ln[(a0 + i) * ES] = o[i];
+                } else {
+#pragma unroll
+                    for (int i = 0; i < K; i++)
+                        if (a0 + i >= 0 && a0 + i < E)
+                            ln[(a0 + i) * ES] = o[i];
+                }
+                if (more) {
+                    pw[0] = own_s;
+                    pw[QS] = X;
+                }
             }
         }
     }
@@ -697,65 +772,75 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
             const int64_t gb = (line0 + q) * a.L + e0;
             if (a.store_quot) {
                 if (a.out_f64) {
-                    double *o_ = reinterpret_cast<double *>(a.out) + gb;
+                    double *o_ = reinterpret_cast<double *>(fp.out) + gb;
                     for (int e = s0 + tid; e < s1; e += nthr) {
                         const C c = c_[e];
                         o_[e] = (double)quotient<Real>(c.x, c.y, thr, offs);
                     }
                 } else {
-                    float *o_ = reinterpret_cast<float *>(a.out) + gb;
+                    float *o_ = reinterpret_cast<float *>(fp.out) + gb;
                     for (int e = s0 + tid; e < s1; e += nthr) {
                         const C c = c_[e];
                         o_[e] = (float)quotient<Real>(c.x, c.y, thr, offs);
                     }
                 }
             } else if (a.plain) {
-                Real *d_ = reinterpret_cast<Real *>(a.dst_v) + gb;
+                Real *d_ = reinterpret_cast<Real *>(fp.dst) + gb;
                 for (int e = s0 + tid; e < s1; e += nthr)
                     d_[e] = c_[e].x;
             } else {
-                C *d_ = reinterpret_cast<C *>(a.dst_v) + gb;
-                for (int e = s0 + tid; e < s1; e += nthr)
-                    d_[e] = c_[e];
+                C *d_ = reinterpret_cast<C *>(fp.dst) + gb;
+                if (sizeof(C) == 8 && ((gb + s0) & 1) == 0 && ((HP + s0) & 1) == 0) {
+                    // pairs of float2 cells as 16-byte vectors
+                    const int np = (s1 - s0) / 2;
+                    const uint4 *sv4 = reinterpret_cast<const uint4 *>(c_ + s0);
+                    uint4 *dv4 = reinterpret_cast<uint4 *>(d_ + s0);
+                    for (int e = tid; e < np; e += nthr)
+                        dv4[e] = sv4[e];
+                    if (((s1 - s0) & 1) && tid == 0)
+                        d_[s1 - 1] = c_[s1 - 1];
+                } else {
+                    for (int e = s0 + tid; e < s1; e += nthr)
+                        d_[e] = c_[e];
+                }
             }
         }
     } else {
         const int64_t es = a.elem_stride;
         const C *dcell = cells + (size_t)HP * G;
         if (a.store_quot) {
-            // one row of G cells per thread: G quotients, one vector store
-            const bool q_vec = G == 4 && vec_ok && (gbase % 4) == 0 && (es % 4) == 0;
-            for (int row = s0 + tid; row < s1; row += nthr) {
-                Real q[G];
+            // two threads per row, G/2 cells (16 bytes of shared memory) each,
+            // so a warp reads 512 consecutive bytes
+            constexpr int HG = G > 1 ? G / 2 : 1;
+            const bool q_vec = HG == 2 && vec_ok && (gbase % 4) == 0 && (es % 4) == 0;
+            for (int i = tid; i < 2 * (s1 - s0); i += nthr) {
+                const int row = s0 + (i >> 1), u0 = (i & 1) * HG;
+                Real q[HG];
 #pragma unroll
-                for (int u = 0; u < G; u++) {
-                    const C c = dcell[row * G + u];
+                for (int u = 0; u < HG; u++) {
+                    const C c = dcell[row * G + u0 + u];
                     q[u] = quotient<Real>(c.x, c.y, thr, offs);
                 }
-                const int64_t gi = gbase + row * es;
+                const int64_t gi = gbase + row * es + u0;
                 if (a.out_f64) {
-                    double *o_ = reinterpret_cast<double *>(a.out) + gi;
+                    double *o_ = reinterpret_cast<double *>(fp.out) + gi;
 #pragma unroll
-                    for (int u = 0; u < G; u++)
-                        if (u < nl)
+                    for (int u = 0; u < HG; u++)
+                        if (u0 + u < nl)
                             o_[u] = (double)q[u];
                 } else if (q_vec) {
-                    float4 v4;
-                    v4.x = (float)q[0];
-                    v4.y = (float)q[1 % G];
-                    v4.z = (float)q[2 % G];
-                    v4.w = (float)q[3 % G];
-                    *reinterpret_cast<float4 *>(reinterpret_cast<float *>(a.out) + gi) = v4;
+                    *reinterpret_cast<float2 *>(reinterpret_cast<float *>(fp.out) + gi) =
+                        make_float2((float)q[0], (float)q[1 % HG]);
                 } else {
-                    float *o_ = reinterpret_cast<float *>(a.out) + gi;
+                    float *o_ = reinterpret_cast<float *>(fp.out) + gi;
 #pragma unroll
-                    for (int u = 0; u < G; u++)
-                        if (u < nl)
+                    for (int u = 0; u < HG; u++)
+                        if (u0 + u < nl)
                             o_[u] = (float)q[u];
                 }
             }
         } else {
-            C *dst = reinterpret_cast<C *>(a.dst_v) + gbase;
+            C *dst = reinterpret_cast<C *>(fp.dst) + gbase;
             if (vec_ok) {
                 const int nv = 2 * (s1 - s0);
                 const uint4 *s_ = reinterpret_cast<const uint4 *>(dcell + (size_t)s0 * G);
@@ -774,58 +859,42 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
     }
 }
 
-// Registers per thread: at most 65536 / (512 * AxisMinBlocks) (the
-// compiler's cap for 512-thread CTAs).
-#ifndef FBG_AXIS_MINB
-#define FBG_AXIS_MINB 1
-#endif
+// Float32 sliding passes with the short chunk fit in 64 registers, so two
+// 512-thread CTAs (or four of 256) can share an SM; the other variants
+// (long chunk, float64 cells, direct sums) keep 128.
+template <typename Real, int K, int MODE>
+struct AxisMinBlocks {
+    static constexpr int value = (sizeof(Real) == 4 && K == K64 && MODE == 0) ? 2 : 1;
+};
 
 template <typename Real, int K, int MODE, int SPLAT_DIM, int LAYOUT>
-__global__ void __launch_bounds__(512, FBG_AXIS_MINB) k_axis(const AxisLaunch a, const Geometry g, const SampleView sv)
+__global__ void __launch_bounds__(512, AxisMinBlocks<Real, K, MODE>::value)
+    k_axis(const AxisLaunch a, const Geometry g, const SampleView sv)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int64_t group = blockIdx.x / a.ntiles;
-    axis_tile<Real, K, MODE, SPLAT_DIM, LAYOUT>(a, g, sv, group, blockIdx.x - group * a.ntiles, smem_raw);
+    TilePtrs fp;
+    fp.src = a.src_v;
+    fp.dst = a.dst_v;
+    fp.out = a.out;
+    fp.bin_start = sv.bin_start;
+    fp.hdr = sv.hdr;
+    axis_tile<Real, K, MODE, SPLAT_DIM, LAYOUT>(a, g, sv, fp, group, blockIdx.x - group * a.ntiles, smem_raw);
 }
 
-// Batched form: the CTAs of one launch take work items (field, block of that
-// field's launch) from a counter until none is left, largest fields first, so
-// fields of uneven size share the GPU without a tail per field.  No CTA waits
-// for another: each item is independent.  The item's field description is
-// copied to shared memory, where every thread reads it.
+// Batched form: fields of identical shape and parameters (one launch
+// description in kernel parameters, one TilePtrs per field); block x of the
+// grid is block x % bpf of field x / bpf.
 template <typename Real, int K, int MODE, int SPLAT_DIM, int LAYOUT>
-__global__ void __launch_bounds__(512, FBG_AXIS_MINB) k_axis_batch(const BatchAxisField *__restrict__ fields,
-                                                                   const BatchItem *__restrict__ items,
-                                                                   uint32_t nitems, uint32_t *__restrict__ counter)
+__global__ void __launch_bounds__(512, AxisMinBlocks<Real, K, MODE>::value)
+    k_axis_batch(const AxisLaunch a, const Geometry g, const SampleView sv, const TilePtrs *__restrict__ fields,
+                 uint32_t blocks_per_field)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ uint32_t s_item;
-    __shared__ __align__(16) BatchAxisField s_f;
-    static_assert(sizeof(BatchAxisField) % 4 == 0, "field copy by words");
-    constexpr int kWords = (int)(sizeof(BatchAxisField) / 4);
-    uint32_t last = 0xFFFFFFFFu;
-    for (;;) {
-        if (threadIdx.x == 0)
-            s_item = atomicAdd(counter, 1u);
-        __syncthreads();
-        const uint32_t it = s_item;
-        if (it >= nitems)
-            break;
-        const BatchItem bi = items[it];
-        if (bi.field != last) {
-            // every thread has passed the barrier above, so no one still reads s_f
-            const uint32_t *src = reinterpret_cast<const uint32_t *>(fields + bi.field);
-            uint32_t *dst = reinterpret_cast<uint32_t *>(&s_f);
-            for (int w = threadIdx.x; w < kWords; w += blockDim.x)
-                dst[w] = src[w];
-            last = bi.field;
-        }
-        __syncthreads();
-        const int64_t group = bi.block / s_f.a.ntiles;
-        axis_tile<Real, K, MODE, SPLAT_DIM, LAYOUT>(s_f.a, s_f.g, s_f.sv, group, bi.block - group * s_f.a.ntiles,
-                                                    smem_raw);
-        __syncthreads();
-    }
+    const uint32_t f = blockIdx.x / blocks_per_field, b = blockIdx.x - f * blocks_per_field;
+    const TilePtrs fp = fields[f];
+    const int64_t group = b / a.ntiles;
+    axis_tile<Real, K, MODE, SPLAT_DIM, LAYOUT>(a, g, sv, fp, group, b - group * a.ntiles, smem_raw);
 }
 
 // ---------------------------------------------------------------------------
@@ -869,40 +938,32 @@ static cudaError_t launch_k(int sd, const AxisLaunch &a, const Geometry &g, cons
 }
 
 template <typename Real, int K, int MODE, int SD, int LAY>
-static cudaError_t launch_batch_one(int op, const BatchAxisField *fields, const BatchItem *items, uint32_t nitems,
-                                    uint32_t *counter, size_t smem, int threads, int *grid, cudaStream_t st)
+static cudaError_t launch_batch_one(int op, const AxisLaunch &a, const Geometry &g, const SampleView &sv,
+                                    const TilePtrs *fields, uint32_t bpf, uint32_t nitems, int *grid, cudaStream_t st)
 {
+    const int prec = sizeof(Real) == 8 ? 0 : 1;
+    const size_t smem = axis_smem_bytes(prec, a);
+    const int threads = axis_threads(prec, a);
     if (op == 1) {
         if (*grid < 1)
             return cudaSuccess;
-        k_axis_batch<Real, K, MODE, SD, LAY><<<(unsigned)*grid, threads, smem, st>>>(fields, items, nitems, counter);
+        k_axis_batch<Real, K, MODE, SD, LAY><<<(unsigned)*grid, threads, smem, st>>>(a, g, sv, fields, bpf);
         return cudaGetLastError();
     }
     cudaError_t e = cudaFuncSetAttribute(k_axis_batch<Real, K, MODE, SD, LAY>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)axis_smem_limit());
-    int per_sm = 0, dev = 0, sms = 0;
-    if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_axis_batch<Real, K, MODE, SD, LAY>, threads,
-                                                          smem);
-    if (e == cudaSuccess)
-        e = cudaGetDevice(&dev);
-    if (e == cudaSuccess)
-        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess)
         return e;
-    if (per_sm < 1)
-        return cudaErrorInvalidConfiguration;
-    *grid = (int)std::min<int64_t>((int64_t)per_sm * sms, (int64_t)nitems);
+    *grid = (int)nitems;
     return cudaSuccess;
 }
 
 template <typename Real, int K, int MODE>
-static cudaError_t launch_batch_k(int op, int sd, int layout, const BatchAxisField *fields, const BatchItem *items,
-                                  uint32_t nitems, uint32_t *counter, size_t smem, int threads, int *grid,
-                                  cudaStream_t st)
+static cudaError_t launch_batch_k(int op, int sd, const AxisLaunch &a, const Geometry &g, const SampleView &sv,
+                                  const TilePtrs *fields, uint32_t bpf, uint32_t nitems, int *grid, cudaStream_t st)
 {
-#define FBG_B(SD, LAY) launch_batch_one<Real, K, MODE, SD, LAY>(op, fields, items, nitems, counter, smem, threads, grid, st)
-    if (layout == 1)
+#define FBG_B(SD, LAY) launch_batch_one<Real, K, MODE, SD, LAY>(op, a, g, sv, fields, bpf, nitems, grid, st)
+    if (a.layout == 1)
         return FBG_B(0, 1);
     switch (sd) {
     case 0: return FBG_B(0, 0);

@@ -703,22 +703,49 @@ extern "C" int fb_resample(const float *d_lam, int64_t lam_w, int64_t lam_h, con
 }
 
 // ---------------------------------------------------------------------------
-// batched 2D fields: one sample sort and one persistent launch per axis stage
+// batched 2D fields: one sample sort and one launch per axis stage
 // for all fields of a plan
 // ---------------------------------------------------------------------------
 
 namespace {
 
-// One persistent launch: the same-shaped axis launches (kernel variant) of
-// several fields, as a table of BatchAxisField and a list of work items.
+// One persistent launch: the s-th axis launch of every field whose launch
+// has the same shape and parameters (everything but the pointers), as one
+// shared launch description and a table of per-field pointers.
 struct BatchStage {
-    int k = 0, mode = 0, sd = 0, layout = 0, axis = 0;
-    size_t smem = 0;
-    int threads = 0;
+    AxisLaunch a{};
+    Geometry g{};
+    SampleView sv{};
+    int axis = 0;
     int grid = 0;
-    size_t off_fields = 0, off_items = 0;
-    uint32_t nitems = 0;
+    size_t off_fields = 0;    // TilePtrs[nf] in the plan's device memory
+    uint32_t nf = 0, bpf = 0, nitems = 0;
 };
+
+bool same_launch(const AxisLaunch &x, const AxisLaunch &y)
+{
+    AxisLaunch u = x, v = y;
+    u.src_v = v.src_v = nullptr;
+    u.src_w = v.src_w = nullptr;
+    u.dst_v = v.dst_v = nullptr;
+    u.dst_w = v.dst_w = nullptr;
+    u.out = v.out = nullptr;
+    // compare field by field (no padding bytes involved)
+    return u.axis == v.axis && u.layout == v.layout && u.L == v.L && u.elem_stride == v.elem_stride &&
+           u.nlines == v.nlines && u.outer_count == v.outer_count && u.outer_stride == v.outer_stride &&
+           u.xblocks == v.xblocks && u.width == v.width && u.lines_per_cta == v.lines_per_cta &&
+           u.tile_len == v.tile_len && u.ntiles == v.ntiles && u.halo == v.halo && u.extent_max == v.extent_max &&
+           u.line_pitch == v.line_pitch && u.line_pad == v.line_pad && u.chunks_pad == v.chunks_pad &&
+           u.part_pitch == v.part_pitch && u.part_pad == v.part_pad && u.passes == v.passes && u.T == v.T &&
+           u.alpha == v.alpha && u.scaled == v.scaled && u.inv_norm == v.inv_norm && u.fill_splat == v.fill_splat &&
+           u.store_quot == v.store_quot && u.out_f64 == v.out_f64 && u.plain == v.plain && u.thr == v.thr &&
+           u.kchunk == v.kchunk && u.rows_threads == v.rows_threads;
+}
+
+bool same_geometry(const Geometry &x, const Geometry &y)
+{
+    return x.dim == y.dim && x.size[0] == y.size[0] && x.size[1] == y.size[1] && x.size[2] == y.size[2];
+}
 
 std::mutex g_batch_tune_mu;
 std::map<std::string, fb_batch_knobs> g_batch_tuned;
@@ -733,7 +760,7 @@ struct fb_batch {
     uint32_t nbins = 0, nblocks = 0;
     char *dev = nullptr;
     size_t dev_bytes = 0;
-    size_t off_keyf = 0, off_blocks = 0, off_hdrs = 0, off_bins = 0, off_sort = 0, off_counters = 0;
+    size_t off_keyf = 0, off_blocks = 0, off_hdrs = 0, off_bins = 0, off_sort = 0;
     std::vector<BatchStage> stages;
     std::vector<fb_field2d> fields;
     cudaStream_t cap = nullptr;
@@ -805,58 +832,53 @@ int batch_build(int precision, const fb_field2d *fields, int nf, int out_f64, fb
             blocks.push_back(make_uint2((unsigned)f, (unsigned)s0));
     b->nblocks = (uint32_t)blocks.size();
 
-    // stages: the s-th launch of every field, grouped by kernel variant;
-    // within a group the fields with most work come first
+    // stages: the s-th launch of every field, grouped by identical launch
+    // shape and parameters
     size_t nstage_max = 0;
     for (const Plan &p : plans)
         nstage_max = std::max(nstage_max, p.launches.size());
-    struct Member {
-        int f;
-        size_t q;
-        int64_t blocks;
-    };
     struct Group {
         BatchStage st;
-        std::vector<Member> m;
+        std::vector<int> f;
+        size_t q = 0;
     };
     std::vector<Group> groups;
     for (size_t q = 0; q < nstage_max; q++) {
-        std::vector<Group> gs;
+        const size_t first = groups.size();
         for (int f = 0; f < nf; f++) {
             if (q >= plans[f].launches.size())
                 continue;
             const AxisLaunch &a = plans[f].launches[q];
-            BatchStage key;
-            key.k = axis_kernel_k(precision, a);
-            key.mode = axis_kernel_mode(precision, a.T);
-            key.sd = a.fill_splat ? 2 : 0;
-            key.layout = a.layout;
-            key.axis = a.axis;
             Group *g = nullptr;
-            for (Group &x : gs)
-                if (x.st.k == key.k && x.st.mode == key.mode && x.st.sd == key.sd && x.st.layout == key.layout)
-                    g = &x;
+            for (size_t x = first; x < groups.size(); x++)
+                if (same_launch(groups[x].st.a, a) && same_geometry(groups[x].st.g, plans[f].g) &&
+                    groups[x].st.sv.nbins == plans[f].nbins && groups[x].st.sv.bin_w == plans[f].bin_w)
+                    g = &groups[x];
             if (!g) {
-                gs.push_back(Group{key, {}});
-                g = &gs.back();
+                Group ng;
+                ng.st.a = a;
+                ng.st.g = plans[f].g;
+                ng.st.sv.nbins = plans[f].nbins;
+                ng.st.sv.bin_w = plans[f].bin_w;
+                ng.st.axis = a.axis;
+                ng.q = q;
+                const int64_t grp = a.layout == 0 ? (a.nlines + a.lines_per_cta - 1) / a.lines_per_cta
+                                                  : a.outer_count * a.xblocks;
+                if (grp * a.ntiles > (int64_t)0x7FFFFFFF)
+                    return fail(FB_ERR_ARG, "field %d: too many blocks in one launch", f);
+                ng.st.bpf = (uint32_t)(grp * a.ntiles);
+                groups.push_back(ng);
+                g = &groups.back();
             }
-            const int64_t grp = a.layout == 0 ? (a.nlines + a.lines_per_cta - 1) / a.lines_per_cta
-                                              : a.outer_count * a.xblocks;
-            g->m.push_back(Member{f, q, grp * a.ntiles});
-            g->st.smem = std::max(g->st.smem, axis_smem_bytes(precision, a));
-            g->st.threads = std::max(g->st.threads, axis_threads(precision, a));
+            g->f.push_back(f);
         }
-        for (Group &g : gs) {
-            std::stable_sort(g.m.begin(), g.m.end(),
-                             [](const Member &x, const Member &y) { return x.blocks > y.blocks; });
-            int64_t items = 0;
-            for (const Member &m : g.m)
-                items += m.blocks;
-            if (items > (int64_t)0xFFFFFFF0ll)
-                return fail(FB_ERR_ARG, "batch stage too large");
-            g.st.nitems = (uint32_t)items;
-            groups.push_back(g);
-        }
+    }
+    for (Group &g : groups) {
+        const int64_t items = (int64_t)g.st.bpf * (int64_t)g.f.size();
+        if (items > (int64_t)0xFFFFFFF0ll)
+            return fail(FB_ERR_ARG, "batch stage too large");
+        g.st.nf = (uint32_t)g.f.size();
+        g.st.nitems = (uint32_t)items;
     }
 
     // device layout
@@ -872,13 +894,9 @@ int batch_build(int precision, const fb_field2d *fields, int nf, int out_f64, fb
     off = align_up(off + sizeof(uint32_t) * ((size_t)nbins + 1));
     b->off_sort = off;
     off = align_up(off + batch_sort_scratch_bytes(ntot, (uint32_t)nbins, precision));
-    b->off_counters = off;
-    off = align_up(off + sizeof(uint32_t) * groups.size());
     for (Group &g : groups) {
         g.st.off_fields = off;
-        off = align_up(off + sizeof(BatchAxisField) * g.m.size());
-        g.st.off_items = off;
-        off = align_up(off + sizeof(BatchItem) * std::max<size_t>(1, g.st.nitems));
+        off = align_up(off + sizeof(TilePtrs) * g.f.size());
     }
     const size_t tables_end = off;
     std::vector<size_t> pair_off((size_t)nf);
@@ -922,43 +940,32 @@ int batch_build(int precision, const fb_field2d *fields, int nf, int out_f64, fb
     batch_sort_views(precision, ntot, (uint32_t)nbins, reinterpret_cast<uint32_t *>(dv + b->off_sort), &sorted,
                      &recs);
     b->stages.clear();
-    for (size_t gi = 0; gi < groups.size(); gi++) {
-        Group &g = groups[gi];
-        BatchAxisField *tf = reinterpret_cast<BatchAxisField *>(img.data() + g.st.off_fields);
-        BatchItem *it = reinterpret_cast<BatchItem *>(img.data() + g.st.off_items);
-        uint32_t ni = 0;
-        for (size_t mi = 0; mi < g.m.size(); mi++) {
-            const Member &m = g.m[mi];
-            const Plan &p = plans[m.f];
-            AxisLaunch a = p.launches[m.q];
+    for (Group &g : groups) {
+        TilePtrs *tp = reinterpret_cast<TilePtrs *>(img.data() + g.st.off_fields);
+        for (size_t mi = 0; mi < g.f.size(); mi++) {
+            const int f = g.f[mi];
+            const AxisLaunch &a = plans[f].launches[g.q];
             auto pair = [&](const void *code) -> void * {
                 const int idx = (int)(intptr_t)code - 16;
-                return idx < 0 ? nullptr : dv + pair_off[m.f] + (size_t)idx * pair_bytes[m.f];
+                return idx < 0 ? nullptr : dv + pair_off[f] + (size_t)idx * pair_bytes[f];
             };
-            a.src_v = pair(a.src_v);
-            a.dst_v = pair(a.dst_v);
-            a.src_w = nullptr;
-            a.dst_w = nullptr;
-            a.out = fields[m.f].out;
-            a.out_f64 = b->out_f64;
-            BatchAxisField &bf = tf[mi];
-            bf.a = a;
-            bf.g = p.g;
-            SampleView sv{};
-            sv.rec = recs;
-            sv.npts = ntot;
-            sv.sorted_idx = sorted;
-            sv.bin_start = reinterpret_cast<const uint32_t *>(dv + b->off_bins) + bin_off[m.f];
-            sv.nbins = p.nbins;
-            sv.bin_w = p.bin_w;
-            sv.hdr = reinterpret_cast<FieldHeader *>(dv + b->off_hdrs) + m.f;
-            bf.sv = sv;
-            for (int64_t k = 0; k < m.blocks; k++)
-                it[ni++] = BatchItem{(uint32_t)mi, (uint32_t)k};
+            tp[mi].src = pair(a.src_v);
+            tp[mi].dst = pair(a.dst_v);
+            tp[mi].out = fields[f].out;
+            tp[mi].bin_start = reinterpret_cast<const uint32_t *>(dv + b->off_bins) + bin_off[f];
+            tp[mi].hdr = reinterpret_cast<const FieldHeader *>(dv + b->off_hdrs) + f;
         }
         BatchStage st = g.st;
-        e = launch_axis_batch(0, precision, st.k, st.mode, st.sd, st.layout, nullptr, nullptr, st.nitems, nullptr,
-                              st.smem, st.threads, &st.grid, nullptr);
+        st.a.src_v = st.a.src_w = nullptr;
+        st.a.dst_v = st.a.dst_w = nullptr;
+        st.a.out = nullptr;
+        st.a.out_f64 = b->out_f64;
+        st.sv.rec = recs;
+        st.sv.npts = ntot;
+        st.sv.sorted_idx = sorted;
+        st.sv.bin_start = nullptr;
+        st.sv.hdr = nullptr;
+        e = launch_axis_batch(0, precision, st.a, st.g, st.sv, nullptr, st.bpf, st.nitems, &st.grid, nullptr);
         if (e != cudaSuccess)
             return cuda_fail(e, "batch axis kernel setup");
         b->stages.push_back(st);
@@ -973,10 +980,7 @@ int batch_enqueue(fb_batch *b, cudaStream_t st, bool prof)
 {
     char *dv = b->dev;
     size_t ev = prof ? prof_event(st) : 0;
-    cudaError_t e = cudaMemsetAsync(dv + b->off_counters, 0, sizeof(uint32_t) * std::max<size_t>(1, b->stages.size()),
-                                    st);
-    if (e != cudaSuccess)
-        return cuda_fail(e, "batch counters");
+    cudaError_t e;
     const uint32_t *sorted = nullptr;
     const void *recs = nullptr;
     e = batch_sort(b->precision, reinterpret_cast<const BatchKeyField *>(dv + b->off_keyf),
@@ -991,13 +995,10 @@ int batch_enqueue(fb_batch *b, cudaStream_t st, bool prof)
         g_prof.recs.push_back({0, ev, e1});
         ev = e1;
     }
-    uint32_t *counters = reinterpret_cast<uint32_t *>(dv + b->off_counters);
     for (size_t i = 0; i < b->stages.size(); i++) {
         BatchStage &s = b->stages[i];
-        e = launch_axis_batch(1, b->precision, s.k, s.mode, s.sd, s.layout,
-                              reinterpret_cast<const BatchAxisField *>(dv + s.off_fields),
-                              reinterpret_cast<const BatchItem *>(dv + s.off_items), s.nitems, counters + i, s.smem,
-                              s.threads, &s.grid, st);
+        e = launch_axis_batch(1, b->precision, s.a, s.g, s.sv, reinterpret_cast<const TilePtrs *>(dv + s.off_fields),
+                              s.bpf, s.nitems, &s.grid, st);
         if (e != cudaSuccess)
             return cuda_fail(e, "batch axis kernel");
         if (prof) {
@@ -1227,15 +1228,15 @@ extern "C" int fb_batch_info(const fb_batch *b, int *kernel_launches, int *memse
         return fail(FB_ERR_ARG, "null plan");
     // batch_sort: k_batch_keys (when there are samples), k_tile_sums,
     // k_scan_exclusive, k_tile_scan, then k_bin_scatter, k_sort_bins,
-    // k_sort_large when there are samples; two memsets; plus the counters'
-    // memset and one persistent launch per stage with work
-    int k = 3 + (b->nblocks > 0 ? 1 : 0) + (b->ntot > 0 ? 3 : 0);
+    // k_sort_large, k_gather_recs when there are samples, and two memsets;
+    // then one axis launch per stage with work
+    int k = 3 + (b->nblocks > 0 ? 1 : 0) + (b->ntot > 0 ? 4 : 0);
     for (const BatchStage &s : b->stages)
         k += s.grid > 0 ? 1 : 0;
     if (kernel_launches)
         *kernel_launches = k;
     if (memsets)
-        *memsets = 3;
+        *memsets = 2;
     if (device_bytes)
         *device_bytes = b->dev_bytes;
     return FB_OK;

@@ -17,6 +17,7 @@ namespace fbg {
 // consecutive chunks of one line hit 32 different shared-memory banks.
 constexpr int K32 = 33;   // float32-compensated form
 constexpr int K64 = 17;   // float64 form (8-byte words: half-warp phases)
+constexpr int K9 = 9;     // float64 sliding passes whose window 2T + 1 is shorter than 17
 
 constexpr int kMaxLineThreads = 1024;
 
@@ -109,10 +110,10 @@ constexpr int kBatchKeysPerBlock = 2048;
 
 // Sorted-sample view handed to the splatting first-axis kernel.
 struct SampleView {
-    const void *rec;              // SampleRec<Real>[npts], by sample index
+    const void *rec;              // SampleRec<Real> in sorted order (by bin, then sample)
     int64_t npts;
-    const uint32_t *sorted_idx;   // sample indices ordered by bin (stable)
-    const uint32_t *bin_start;    // nbins + 1 offsets into sorted_idx
+    const uint32_t *sorted_idx;   // sample indices in the same order
+    const uint32_t *bin_start;    // nbins + 1 offsets into rec / sorted_idx
     uint32_t nbins;
     int bin_w;                    // 1D only: cells per bin
     const FieldHeader *hdr;
@@ -163,16 +164,14 @@ struct AxisLaunch {
     int rows_threads;         // rows layout: target threads per CTA (0 = 256)
 };
 
-// One field of a batched axis launch, and one CTA's share of work in it
-// (a line group / tile of that field).
-struct BatchAxisField {
-    AxisLaunch a;
-    Geometry g;
-    SampleView sv;
-};
-struct BatchItem {
-    uint32_t field;
-    uint32_t block;
+// The pointers that differ between the fields of a batched axis launch (the
+// rest of the launch description is shared and lives in kernel parameters).
+struct TilePtrs {
+    const void *src;              // input (v, w) cells (or plain lines)
+    void *dst;                    // output (v, w) cells (or plain lines)
+    void *out;                    // quotient output
+    const uint32_t *bin_start;    // sorted-sample bin starts of the field
+    const FieldHeader *hdr;       // value range of the field
 };
 
 }  // namespace fbg

@@ -35,17 +35,13 @@ size_t axis_smem_bytes(int precision, const AxisLaunch &a);
 bool axis_shape(int precision, AxisLaunch &a);
 cudaError_t launch_axis(int precision, const AxisLaunch &a, const Geometry &g, const SampleView &sv,
                         cudaStream_t st);
-// Batched launches (structures in fb_axis_impl.cuh).
-struct BatchAxisField;
-struct BatchItem;
-int axis_kernel_k(int precision, const AxisLaunch &a);
-int axis_kernel_mode(int precision, int T);
+// Batched launches: fields of one launch share `a`, `g` and `sv` except for
+// the pointers in fields[] (bpf blocks per field, nitems blocks in all).
+// op 0: set the kernel's shared-memory limit and return the grid in *grid;
+// op 1: launch it.
 int axis_threads(int precision, const AxisLaunch &a);
-// op 0: set the kernel's shared-memory limit and return in *grid the
-// persistent grid (resident CTAs x SMs, at most nitems); op 1: launch it.
-cudaError_t launch_axis_batch(int op, int precision, int k, int mode, int sd, int layout,
-                              const BatchAxisField *fields, const BatchItem *items, uint32_t nitems,
-                              uint32_t *counter, size_t smem, int threads, int *grid, cudaStream_t st);
+cudaError_t launch_axis_batch(int op, int precision, const AxisLaunch &a, const Geometry &g, const SampleView &sv,
+                              const TilePtrs *fields, uint32_t bpf, uint32_t nitems, int *grid, cudaStream_t st);
 // Tuning knobs ("chunk": 0 automatic, 17 or 33); returns 0 if accepted.
 int axis_tune(const char *name, int value);
 // Standalone n-pass box filter over contiguous device lines (no splat, no

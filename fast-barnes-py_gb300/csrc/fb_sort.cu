@@ -22,6 +22,42 @@ namespace fbg {
 // values.  The header and the counts start zeroed (min is kept complemented
 // for that reason).  The float64 form divides by the step like the reference
 // (interpolation.py:247-248); the float32 form multiplies by its reciprocal.
+// Block-wide reduction of the value range (order-preserving integer keys)
+// and the NaN flag, then one set of atomics per block on the field header.
+__device__ __forceinline__ void range_to_header(unsigned long long kmin, unsigned long long kmax, int nan,
+                                                FieldHeader *hdr)
+{
+    __shared__ unsigned long long s_min[32], s_max[32];
+    __shared__ int s_nan[32];
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long a = __shfl_xor_sync(0xffffffffu, kmin, o);
+        unsigned long long b = __shfl_xor_sync(0xffffffffu, kmax, o);
+        kmin = a < kmin ? a : kmin;
+        kmax = b > kmax ? b : kmax;
+    }
+    nan = __any_sync(0xffffffffu, nan);
+    const int w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        s_min[w] = kmin;
+        s_max[w] = kmax;
+        s_nan[w] = nan;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 1; q < nw; q++) {
+            kmin = s_min[q] < kmin ? s_min[q] : kmin;
+            kmax = s_max[q] > kmax ? s_max[q] : kmax;
+            nan |= s_nan[q];
+        }
+        if (kmin != ~0ull)
+            atomicMax(&hdr->vmin_key, ~kmin);
+        if (kmax != 0ull)
+            atomicMax(&hdr->vmax_key, kmax);
+        if (nan)
+            atomicExch(&hdr->nan_seen, 1);
+    }
+}
+
 template <int DIM, typename Real>
 __global__ void k_bin_keys(const double *__restrict__ pts, const double *__restrict__ val, int64_t npts,
                            Geometry g, int bin_w, uint32_t nbins, uint32_t *__restrict__ keys,
@@ -78,21 +114,7 @@ __global__ void k_bin_keys(const double *__restrict__ pts, const double *__restr
         if (key < nbins)
             atomicAdd(&counts[key], 1u);
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        unsigned long long a = __shfl_xor_sync(0xffffffffu, kmin, o);
-        unsigned long long b = __shfl_xor_sync(0xffffffffu, kmax, o);
-        kmin = a < kmin ? a : kmin;
-        kmax = b > kmax ? b : kmax;
-    }
-    nan = __any_sync(0xffffffffu, nan);
-    if ((threadIdx.x & 31) == 0) {
-        if (kmin != ~0ull)
-            atomicMax(&hdr->vmin_key, ~kmin);
-        if (kmax != 0ull)
-            atomicMax(&hdr->vmax_key, kmax);
-        if (nan)
-            atomicExch(&hdr->nan_seen, 1);
-    }
+    range_to_header(kmin, kmax, nan, hdr);
 }
 
 // Exclusive prefix sum of n entries, one block of 1024 threads walking tiles
@@ -319,22 +341,7 @@ __global__ void k_batch_keys(const BatchKeyField *__restrict__ fields, const uin
         if (key < skip_key)
             atomicAdd(&counts[key], 1u);
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        unsigned long long a = __shfl_xor_sync(0xffffffffu, kmin, o);
-        unsigned long long b = __shfl_xor_sync(0xffffffffu, kmax, o);
-        kmin = a < kmin ? a : kmin;
-        kmax = b > kmax ? b : kmax;
-    }
-    nan = __any_sync(0xffffffffu, nan);
-    if ((threadIdx.x & 31) == 0) {
-        FieldHeader *hdr = hdrs + bt.x;
-        if (kmin != ~0ull)
-            atomicMax(&hdr->vmin_key, ~kmin);
-        if (kmax != 0ull)
-            atomicMax(&hdr->vmax_key, kmax);
-        if (nan)
-            atomicExch(&hdr->nan_seen, 1);
-    }
+    range_to_header(kmin, kmax, nan, hdrs + bt.x);
 }
 
 // Device-wide exclusive scan in three steps: sums of 4096-entry tiles, an
@@ -410,99 +417,155 @@ __global__ void __launch_bounds__(1024) k_tile_scan(const uint32_t *__restrict__
     }
 }
 
+// Records in sorted order: the splat then reads each line's records as one
+// contiguous run instead of gathering them through the index list.
+template <typename Real>
+__global__ void k_gather_recs(const uint32_t *__restrict__ bin_start, uint32_t nbins,
+                              const uint32_t *__restrict__ sorted, const SampleRec<Real> *__restrict__ rec,
+                              SampleRec<Real> *__restrict__ out)
+{
+    const uint32_t total = bin_start[nbins];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x)
+        out[i] = rec[sorted[i]];
+}
+
+// Scratch layout: counts[nbins + 2] | cursor[nbins + 2] | large[nbins + 2] |
+// keys[N] | sorted[N] | big-bin scratch[2N] (uint32), then the sample records
+// by sample index, the records in sorted order, and (batched form) the
+// per-tile sums of the device-wide scan.
+namespace {
+struct SortLayout {
+    uint32_t *counts, *cursor, *large, *keys, *sorted, *big, *tsum;
+    char *rec, *srec;
+    size_t bytes;   // through the sorted records
+};
+
+size_t rec_bytes(int precision) { return precision == 0 ? sizeof(SampleRec<double>) : sizeof(SampleRec<float>); }
+size_t up256(size_t x) { return (x + 255) / 256 * 256; }
+
+// Byte offsets of the record arrays and of the end of the sorted records.
+void sort_offsets(int64_t n, uint32_t nbins, int precision, size_t &rec, size_t &srec, size_t &end)
+{
+    const size_t nb = (size_t)nbins + 2;
+    rec = up256(4 * (3 * nb + 4 * (size_t)n));
+    srec = rec + up256(rec_bytes(precision) * (size_t)n);
+    end = srec + up256(rec_bytes(precision) * (size_t)n);
+}
+
+SortLayout sort_layout(uint32_t *scratch, int64_t n, uint32_t nbins, int precision)
+{
+    SortLayout l;
+    const size_t nb = (size_t)nbins + 2;
+    l.counts = scratch;
+    l.cursor = l.counts + nb;
+    l.large = l.cursor + nb;
+    l.keys = l.large + nb;
+    l.sorted = l.keys + n;
+    l.big = l.sorted + n;
+    size_t rec, srec, end;
+    sort_offsets(n, nbins, precision, rec, srec, end);
+    char *base = reinterpret_cast<char *>(scratch);
+    l.rec = base + rec;
+    l.srec = base + srec;
+    l.tsum = reinterpret_cast<uint32_t *>(base + end);
+    l.bytes = end;
+    return l;
+}
+}  // namespace
+
+size_t sort_scratch_bytes(int64_t npts, uint32_t nbins, int precision)
+{
+    size_t rec, srec, end;
+    sort_offsets(npts, nbins, precision, rec, srec, end);
+    return end + 256;
+}
+
 size_t batch_sort_scratch_bytes(int64_t ntot, uint32_t nbins, int precision)
 {
     const size_t tiles = ((size_t)nbins + 1 + 4095) / 4096;
-    return sort_scratch_bytes(ntot, nbins, precision) + 8 * tiles + 256;
+    size_t rec, srec, end;
+    sort_offsets(ntot, nbins, precision, rec, srec, end);
+    return end + 8 * tiles + 256;
 }
 
 void batch_sort_views(int precision, int64_t ntot, uint32_t nbins, uint32_t *scratch, const uint32_t **sorted_idx,
                       const void **recs)
 {
-    const size_t words = 3 * ((size_t)nbins + 2) + 4 * (size_t)ntot;
-    *sorted_idx = scratch + 3 * ((size_t)nbins + 2) + (size_t)ntot;
-    *recs = reinterpret_cast<char *>(scratch) + (4 * words + 255) / 256 * 256;
-    (void)precision;
+    const SortLayout l = sort_layout(scratch, ntot, nbins, precision);
+    *sorted_idx = l.sorted;
+    *recs = l.srec;
+}
+
+static void gather_recs(int precision, const SortLayout &l, const uint32_t *bin_start, uint32_t nbins, int64_t n,
+                        cudaStream_t st)
+{
+    const int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
+    if (precision == 0)
+        k_gather_recs<double><<<blocks, 256, 0, st>>>(bin_start, nbins, l.sorted,
+                                                       reinterpret_cast<const SampleRec<double> *>(l.rec),
+                                                       reinterpret_cast<SampleRec<double> *>(l.srec));
+    else
+        k_gather_recs<float><<<blocks, 256, 0, st>>>(bin_start, nbins, l.sorted,
+                                                      reinterpret_cast<const SampleRec<float> *>(l.rec),
+                                                      reinterpret_cast<SampleRec<float> *>(l.srec));
 }
 
 cudaError_t batch_sort(int precision, const BatchKeyField *d_fields, const uint2 *d_blocks, uint32_t nblocks,
                        int64_t ntot, uint32_t nbins, FieldHeader *hdrs, int nfields, uint32_t *scratch,
                        uint32_t *bin_start, const uint32_t **sorted_idx, const void **recs, cudaStream_t st)
 {
-    uint32_t *counts = scratch;
-    uint32_t *cursor = counts + (nbins + 2);
-    uint32_t *large = cursor + (nbins + 2);
-    uint32_t *keys = large + (nbins + 2);
-    uint32_t *sorted = keys + ntot;
-    uint32_t *big = sorted + ntot;
-    const size_t words = 3 * ((size_t)nbins + 2) + 4 * (size_t)ntot;
-    char *rec = reinterpret_cast<char *>(scratch) + (4 * words + 255) / 256 * 256;
-    const size_t recb = precision == 0 ? sizeof(SampleRec<double>) : sizeof(SampleRec<float>);
-    uint32_t *tsum = reinterpret_cast<uint32_t *>(rec + ((recb * (size_t)ntot + 255) / 256 * 256));
+    const SortLayout l = sort_layout(scratch, ntot, nbins, precision);
     cudaError_t e = cudaMemsetAsync(hdrs, 0, sizeof(FieldHeader) * (size_t)nfields, st);
     if (e == cudaSuccess)
-        e = cudaMemsetAsync(counts, 0, sizeof(uint32_t) * 3 * ((size_t)nbins + 2), st);
+        e = cudaMemsetAsync(l.counts, 0, sizeof(uint32_t) * 3 * ((size_t)nbins + 2), st);
     if (e != cudaSuccess)
         return e;
-    *sorted_idx = sorted;
-    *recs = rec;
+    *sorted_idx = l.sorted;
+    *recs = l.srec;
     if (nblocks > 0) {
         if (precision == 0)
-            k_batch_keys<double><<<nblocks, 256, 0, st>>>(d_fields, d_blocks, nbins, keys,
-                                                           reinterpret_cast<SampleRec<double> *>(rec), counts, hdrs);
+            k_batch_keys<double><<<nblocks, 256, 0, st>>>(d_fields, d_blocks, nbins, l.keys,
+                                                           reinterpret_cast<SampleRec<double> *>(l.rec), l.counts,
+                                                           hdrs);
         else
-            k_batch_keys<float><<<nblocks, 256, 0, st>>>(d_fields, d_blocks, nbins, keys,
-                                                          reinterpret_cast<SampleRec<float> *>(rec), counts, hdrs);
+            k_batch_keys<float><<<nblocks, 256, 0, st>>>(d_fields, d_blocks, nbins, l.keys,
+                                                          reinterpret_cast<SampleRec<float> *>(l.rec), l.counts,
+                                                          hdrs);
     }
     const int64_t n = (int64_t)nbins + 1;
     const unsigned tiles = (unsigned)((n + 4095) / 4096);
-    k_tile_sums<<<tiles, 1024, 0, st>>>(counts, n, tsum);
-    uint32_t *toff = tsum + tiles;
-    k_scan_exclusive<<<1, 1024, 0, st>>>(tsum, toff, (int64_t)tiles);
-    k_tile_scan<<<tiles, 1024, 0, st>>>(counts, n, toff, bin_start);
+    k_tile_sums<<<tiles, 1024, 0, st>>>(l.counts, n, l.tsum);
+    uint32_t *toff = l.tsum + tiles;
+    k_scan_exclusive<<<1, 1024, 0, st>>>(l.tsum, toff, (int64_t)tiles);
+    k_tile_scan<<<tiles, 1024, 0, st>>>(l.counts, n, toff, bin_start);
     if (ntot > 0) {
         int blocks = (int)std::min<int64_t>((ntot + 255) / 256, 152 * 8);
-        k_bin_scatter<<<blocks, 256, 0, st>>>(keys, ntot, nbins, bin_start, cursor, sorted);
+        k_bin_scatter<<<blocks, 256, 0, st>>>(l.keys, ntot, nbins, bin_start, l.cursor, l.sorted);
         k_sort_bins<<<(unsigned)((nbins + kBinSortWarps - 1) / kBinSortWarps), 32 * kBinSortWarps, 0, st>>>(
-            bin_start, nbins, sorted, large);
-        k_sort_large<<<64, 1024, 0, st>>>(bin_start, sorted, large, big);
+            bin_start, nbins, l.sorted, l.large);
+        k_sort_large<<<64, 1024, 0, st>>>(bin_start, l.sorted, l.large, l.big);
+        gather_recs(precision, l, bin_start, nbins, ntot, st);
     }
     return cudaGetLastError();
-}
-
-// Scratch layout: counts[nbins + 2] | cursor[nbins + 2] | large[nbins + 2] |
-// keys[N] | sorted[N] | big-bin scratch[2N] (uint32), then the sample records.
-size_t sort_scratch_bytes(int64_t npts, uint32_t nbins, int precision)
-{
-    const size_t words = 3 * ((size_t)nbins + 2) + 4 * (size_t)npts;
-    const size_t rec = precision == 0 ? sizeof(SampleRec<double>) : sizeof(SampleRec<float>);
-    return (4 * words + 255) / 256 * 256 + rec * (size_t)npts + 256;
 }
 
 cudaError_t sort_samples(int precision, const double *pts, const double *val, int64_t npts, const Geometry &g,
                          int bin_w, uint32_t nbins, FieldHeader *hdr, uint32_t *scratch, uint32_t *bin_start,
                          const uint32_t **sorted_idx, const void **recs, cudaStream_t st)
 {
-    uint32_t *counts = scratch;
-    uint32_t *cursor = counts + (nbins + 2);
-    uint32_t *large = cursor + (nbins + 2);
-    uint32_t *keys = large + (nbins + 2);
-    uint32_t *sorted = keys + npts;
-    uint32_t *big = sorted + npts;
-    const size_t words = 3 * ((size_t)nbins + 2) + 4 * (size_t)npts;
-    void *rec = reinterpret_cast<char *>(scratch) + (4 * words + 255) / 256 * 256;
+    const SortLayout l = sort_layout(scratch, npts, nbins, precision);
     cudaError_t e = cudaMemsetAsync(hdr, 0, sizeof(FieldHeader), st);
     if (e == cudaSuccess)
-        e = cudaMemsetAsync(counts, 0, sizeof(uint32_t) * 3 * ((size_t)nbins + 2), st);
+        e = cudaMemsetAsync(l.counts, 0, sizeof(uint32_t) * 3 * ((size_t)nbins + 2), st);
     if (e != cudaSuccess)
         return e;
-    *sorted_idx = sorted;
-    *recs = rec;
+    *sorted_idx = l.sorted;
+    *recs = l.srec;
     if (npts > 0) {
         int blocks = (int)std::min<int64_t>((npts + 255) / 256, 152 * 8);
 #define FBG_KEYS(D, R)                                                                                            \
-    k_bin_keys<D, R><<<blocks, 256, 0, st>>>(pts, val, npts, g, bin_w, nbins, keys,                                \
-                                             reinterpret_cast<SampleRec<R> *>(rec), counts, hdr)
+    k_bin_keys<D, R><<<blocks, 256, 0, st>>>(pts, val, npts, g, bin_w, nbins, l.keys,                              \
+                                             reinterpret_cast<SampleRec<R> *>(l.rec), l.counts, hdr)
         if (precision == 0) {
             if (g.dim == 1)
                 FBG_KEYS(1, double);
@@ -520,13 +583,14 @@ cudaError_t sort_samples(int precision, const double *pts, const double *val, in
         }
 #undef FBG_KEYS
     }
-    k_scan_exclusive<<<1, 1024, 0, st>>>(counts, bin_start, (int64_t)nbins + 1);
+    k_scan_exclusive<<<1, 1024, 0, st>>>(l.counts, bin_start, (int64_t)nbins + 1);
     if (npts > 0) {
         int blocks = (int)std::min<int64_t>((npts + 255) / 256, 152 * 8);
-        k_bin_scatter<<<blocks, 256, 0, st>>>(keys, npts, nbins, bin_start, cursor, sorted);
+        k_bin_scatter<<<blocks, 256, 0, st>>>(l.keys, npts, nbins, bin_start, l.cursor, l.sorted);
         k_sort_bins<<<(unsigned)((nbins + kBinSortWarps - 1) / kBinSortWarps), 32 * kBinSortWarps, 0, st>>>(
-            bin_start, nbins, sorted, large);
-        k_sort_large<<<64, 1024, 0, st>>>(bin_start, sorted, large, big);
+            bin_start, nbins, l.sorted, l.large);
+        k_sort_large<<<64, 1024, 0, st>>>(bin_start, l.sorted, l.large, l.big);
+        gather_recs(precision, l, bin_start, nbins, npts, st);
     }
     return cudaGetLastError();
 }

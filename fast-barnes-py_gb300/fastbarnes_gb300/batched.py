@@ -4,7 +4,7 @@ fastbarnes/interpolation.py:36).
 
 A :class:`BatchPlan` holds the device inputs and outputs of many independent
 2D fields -- each with its own samples, sigma, grid and method -- and runs all
-of them with one sample sort and one persistent launch per axis, optionally
+of them with one sample sort and one launch per axis stage, optionally
 replayed from a CUDA graph.  Each field's result equals
 ``interpolation.barnes(..., precision=p)`` of that field.
 

@@ -113,8 +113,9 @@ int fb_profile_end(int *stages, float *ms, int max_records, int *n_records);
  * (fastbarnes/interpolation.py:36 barnes; a batch is a Python loop over it,
  * demo/timing1_table1_figure4.py:107-115).  A plan holds many independent 2D
  * fields (each its own samples, sigma, grid and output, optimized convolution
- * or convolution) and runs all of them with one sample sort and one persistent
- * launch per axis.  Every field's result equals that of fb_interpolate on it.
+ * or convolution) and runs all of them with one sample sort and, per axis
+ * stage, one launch for every set of fields of identical grid and parameters.
+ * Every field's result equals that of fb_interpolate on it.
  *
  * fb_batch_create checks the fields, plans the launches and allocates the
  * plan's device memory (tables, sort scratch, intermediate fields) on the
