@@ -405,7 +405,8 @@ def main():
                 "data": "synthetic (seeded uniform samples, smooth field + noise)",
                 "config": workload_config(B, args.precision) | {"parallelism": f"replicas x{world}",
                                                                  "knobs": {"chunk": knobs[0],
-                                                                           "rows_threads": knobs[1]}},
+                                                                           "rows_threads": knobs[1],
+                                                                           "mixed": knobs[2]}},
                 "gpu_launches": launches_per_step * args.steps,
                 "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
                              "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,

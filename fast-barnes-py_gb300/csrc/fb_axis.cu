@@ -170,6 +170,24 @@ cudaError_t launch_axis_batch_f64(int op, int k, int mode, int sd, const AxisLau
                                   int *grid, cudaStream_t st);
 
 
+cudaError_t launch_axis_mixed_f32(int op, int k, int mode, int sd, int layout, const MixedField *fields,
+                                  const uint2 *items, uint32_t nitems, size_t smem, int threads, cudaStream_t st);
+cudaError_t launch_axis_mixed_f64(int op, int k, int mode, int sd, int layout, const MixedField *fields,
+                                  const uint2 *items, uint32_t nitems, size_t smem, int threads, cudaStream_t st);
+
+int axis_variant_k(int precision, const AxisLaunch &a) { return kchunk_of(precision, a.T, a.kchunk); }
+int axis_variant_mode(int precision, const AxisLaunch &a) { return direct_mode(precision, a.T) ? 1 : 0; }
+
+cudaError_t launch_axis_mixed(int op, int precision, int k, int mode, int sd, int layout, const MixedField *fields,
+                              const uint2 *items, uint32_t nitems, size_t smem, int threads, cudaStream_t st)
+{
+    if (layout == 1 && sd != 0)
+        return cudaErrorInvalidValue;
+    if (precision == 0)
+        return launch_axis_mixed_f64(op, k, mode, sd, layout, fields, items, nitems, smem, threads, st);
+    return launch_axis_mixed_f32(op, k, mode, sd, layout, fields, items, nitems, smem, threads, st);
+}
+
 cudaError_t launch_axis_batch(int op, int precision, const AxisLaunch &a, const Geometry &g, const SampleView &sv,
                               const TilePtrs *fields, uint32_t bpf, uint32_t nitems, int *grid, cudaStream_t st)
 {

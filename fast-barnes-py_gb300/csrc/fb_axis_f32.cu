@@ -31,4 +31,17 @@ cudaError_t launch_axis_batch_f32(int op, int k, int mode, int sd, const AxisLau
     return launch_axis_batch_f32l(op, sd, a, g, sv, fields, bpf, nitems, grid, st);
 }
 
+cudaError_t launch_axis_mixed_f32l(int op, int sd, int layout, const MixedField *fields, const uint2 *items,
+                                   uint32_t nitems, size_t smem, int threads, cudaStream_t st);
+
+cudaError_t launch_axis_mixed_f32(int op, int k, int mode, int sd, int layout, const MixedField *fields,
+                                  const uint2 *items, uint32_t nitems, size_t smem, int threads, cudaStream_t st)
+{
+    if (mode == 1)
+        return launch_mixed_k<float, K64, 1>(op, sd, layout, fields, items, nitems, smem, threads, st);
+    if (k == K64)
+        return launch_mixed_k<float, K64, 0>(op, sd, layout, fields, items, nitems, smem, threads, st);
+    return launch_axis_mixed_f32l(op, sd, layout, fields, items, nitems, smem, threads, st);
+}
+
 }  // namespace fbg

@@ -16,4 +16,10 @@ cudaError_t launch_axis_batch_f32l(int op, int sd, const AxisLaunch &a, const Ge
     return launch_batch_k<float, K32, 0>(op, sd, a, g, sv, fields, bpf, nitems, grid, st);
 }
 
+cudaError_t launch_axis_mixed_f32l(int op, int sd, int layout, const MixedField *fields, const uint2 *items,
+                                   uint32_t nitems, size_t smem, int threads, cudaStream_t st)
+{
+    return launch_mixed_k<float, K32, 0>(op, sd, layout, fields, items, nitems, smem, threads, st);
+}
+
 }  // namespace fbg

@@ -9,6 +9,19 @@ cudaError_t launch_axis_batch_f64s(int op, int sd, const AxisLaunch &a, const Ge
                                    const TilePtrs *fields, uint32_t bpf, uint32_t nitems, int *grid,
                                    cudaStream_t st);
 
+cudaError_t launch_axis_mixed_f64s(int op, int sd, int layout, const MixedField *fields, const uint2 *items,
+                                   uint32_t nitems, size_t smem, int threads, cudaStream_t st);
+
+cudaError_t launch_axis_mixed_f64(int op, int k, int mode, int sd, int layout, const MixedField *fields,
+                                  const uint2 *items, uint32_t nitems, size_t smem, int threads, cudaStream_t st)
+{
+    if (mode == 1)
+        return launch_mixed_k<double, K64, 1>(op, sd, layout, fields, items, nitems, smem, threads, st);
+    if (k == K9)
+        return launch_axis_mixed_f64s(op, sd, layout, fields, items, nitems, smem, threads, st);
+    return launch_mixed_k<double, K64, 0>(op, sd, layout, fields, items, nitems, smem, threads, st);
+}
+
 cudaError_t launch_axis_f64(int k, int mode, int sd, const AxisLaunch &a, const Geometry &g, const SampleView &sv,
                             cudaStream_t st)
 {

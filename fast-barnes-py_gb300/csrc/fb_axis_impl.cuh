@@ -313,12 +313,17 @@ __device__ __forceinline__ void clip_chunk(C (&o)[K], int a, int E)
 
 // NaN where the weight is below the mask level, else vg / wg + offset
 // (interpolation.py:428-430, :367); `offset` already in the form's precision.
+// The float32 form divides with __fdividef (within 2 ulp; the weights stay
+// far below its 2^126 limit: unscaled sums are capped at 1e24 by the plan).
+__device__ __forceinline__ double quotient_div(double v, double w) { return v / w; }
+__device__ __forceinline__ float quotient_div(float v, float w) { return __fdividef(v, w); }
+
 template <typename Real>
 __device__ __forceinline__ Real quotient(Real v, Real w, Real thr, Real offset)
 {
     const Real nan = sizeof(Real) == 8 ? (Real)__longlong_as_double(0x7ff8000000000000ll)
                                        : (Real)__int_as_float(0x7fc00000);
-    return (w < thr) ? nan : v / w + offset;
+    return (w < thr) ? nan : quotient_div(v, w) + offset;
 }
 
 // ---------------------------------------------------------------------------
@@ -897,6 +902,30 @@ __global__ void __launch_bounds__(512, AxisMinBlocks<Real, K, MODE>::value)
     axis_tile<Real, K, MODE, SPLAT_DIM, LAYOUT>(a, g, sv, fp, group, b - group * a.ntiles, smem_raw);
 }
 
+// Mixed batched form: one launch for fields of different grids and
+// parameters (same kernel variant).  Block x works on items[x] = (field,
+// block of that field's launch); the field's description is copied to shared
+// memory first.  Items are ordered largest field first.
+template <typename Real, int K, int MODE, int SPLAT_DIM, int LAYOUT>
+__global__ void __launch_bounds__(512, AxisMinBlocks<Real, K, MODE>::value)
+    k_axis_mixed(const MixedField *__restrict__ fields, const uint2 *__restrict__ items)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ __align__(16) MixedField s_f;
+    static_assert(sizeof(MixedField) % 4 == 0, "field copy by words");
+    const uint2 it = items[blockIdx.x];
+    {
+        const uint32_t *src = reinterpret_cast<const uint32_t *>(fields + it.x);
+        uint32_t *dst = reinterpret_cast<uint32_t *>(&s_f);
+        for (int w = threadIdx.x; w < (int)(sizeof(MixedField) / 4); w += blockDim.x)
+            dst[w] = src[w];
+    }
+    __syncthreads();
+    const int64_t group = it.y / s_f.a.ntiles;
+    axis_tile<Real, K, MODE, SPLAT_DIM, LAYOUT>(s_f.a, s_f.g, s_f.sv, s_f.fp, group, it.y - group * s_f.a.ntiles,
+                                                smem_raw);
+}
+
 // ---------------------------------------------------------------------------
 // launch templates
 // ---------------------------------------------------------------------------
@@ -956,6 +985,36 @@ static cudaError_t launch_batch_one(int op, const AxisLaunch &a, const Geometry 
         return e;
     *grid = (int)nitems;
     return cudaSuccess;
+}
+
+template <typename Real, int K, int MODE, int SD, int LAY>
+static cudaError_t launch_mixed_one(int op, const MixedField *fields, const uint2 *items, uint32_t nitems,
+                                    size_t smem, int threads, cudaStream_t st)
+{
+    if (op == 1) {
+        if (nitems < 1)
+            return cudaSuccess;
+        k_axis_mixed<Real, K, MODE, SD, LAY><<<nitems, threads, smem, st>>>(fields, items);
+        return cudaGetLastError();
+    }
+    return cudaFuncSetAttribute(k_axis_mixed<Real, K, MODE, SD, LAY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)axis_smem_limit());
+}
+
+template <typename Real, int K, int MODE>
+static cudaError_t launch_mixed_k(int op, int sd, int layout, const MixedField *fields, const uint2 *items,
+                                  uint32_t nitems, size_t smem, int threads, cudaStream_t st)
+{
+#define FBG_M(SD, LAY) launch_mixed_one<Real, K, MODE, SD, LAY>(op, fields, items, nitems, smem, threads, st)
+    if (layout == 1)
+        return FBG_M(0, 1);
+    switch (sd) {
+    case 0: return FBG_M(0, 0);
+    case 1: return FBG_M(1, 0);
+    case 2: return FBG_M(2, 0);
+    default: return FBG_M(3, 0);
+    }
+#undef FBG_M
 }
 
 template <typename Real, int K, int MODE>

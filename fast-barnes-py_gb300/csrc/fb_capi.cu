@@ -713,12 +713,17 @@ namespace {
 // has the same shape and parameters (everything but the pointers), as one
 // shared launch description and a table of per-field pointers.
 struct BatchStage {
-    AxisLaunch a{};
+    bool mixed = false;       // fields of different shapes: MixedField table + items
+    AxisLaunch a{};           // homogeneous: the shared launch description
     Geometry g{};
     SampleView sv{};
+    int k = 0, mode = 0, sd = 0, layout = 0;   // kernel variant
+    size_t smem = 0;          // mixed: largest shared memory of its fields
+    int threads = 0;          // mixed: most threads of its fields
     int axis = 0;
     int grid = 0;
-    size_t off_fields = 0;    // TilePtrs[nf] in the plan's device memory
+    size_t off_fields = 0;    // TilePtrs[nf] (homogeneous) or MixedField[nf] (mixed)
+    size_t off_items = 0;     // mixed: uint2 (field, block)[nitems]
     uint32_t nf = 0, bpf = 0, nitems = 0;
 };
 
@@ -754,7 +759,7 @@ std::map<std::string, fb_batch_knobs> g_batch_tuned;
 
 struct fb_batch {
     int precision = 1, out_f64 = 0, flags = 0, device = 0;
-    fb_batch_knobs knobs{0, 0};
+    fb_batch_knobs knobs{0, 0, 0};
     int nfields = 0;
     int64_t ntot = 0;
     uint32_t nbins = 0, nblocks = 0;
@@ -794,6 +799,8 @@ int batch_build(int precision, const fb_field2d *fields, int nf, int out_f64, fb
         return fail(FB_ERR_ARG, "chunk must be 0, 17 or 33 (got %d)", kn.chunk);
     if (kn.rows_threads != 0 && kn.rows_threads != 128 && kn.rows_threads != 256 && kn.rows_threads != 512)
         return fail(FB_ERR_ARG, "rows_threads must be 0, 128, 256 or 512 (got %d)", kn.rows_threads);
+    if (kn.mixed != 0 && kn.mixed != 1)
+        return fail(FB_ERR_ARG, "mixed must be 0 or 1 (got %d)", kn.mixed);
     b->precision = precision;
     b->out_f64 = out_f64 ? 1 : 0;
     b->knobs = kn;
@@ -832,15 +839,23 @@ int batch_build(int precision, const fb_field2d *fields, int nf, int out_f64, fb
             blocks.push_back(make_uint2((unsigned)f, (unsigned)s0));
     b->nblocks = (uint32_t)blocks.size();
 
-    // stages: the s-th launch of every field, grouped by identical launch
-    // shape and parameters
+    // stages: the s-th launch of every field, grouped by kernel variant; a
+    // group whose fields all have the same shape and parameters shares one
+    // launch description (unless the knobs ask for mixed launches), any
+    // other group goes through a table of per-field descriptions
     size_t nstage_max = 0;
     for (const Plan &p : plans)
         nstage_max = std::max(nstage_max, p.launches.size());
     struct Group {
         BatchStage st;
         std::vector<int> f;
+        std::vector<uint32_t> fblocks;   // blocks of each field's launch
         size_t q = 0;
+    };
+    auto blocks_of = [](const AxisLaunch &a) -> int64_t {
+        const int64_t grp = a.layout == 0 ? (a.nlines + a.lines_per_cta - 1) / a.lines_per_cta
+                                          : a.outer_count * a.xblocks;
+        return grp * a.ntiles;
     };
     std::vector<Group> groups;
     for (size_t q = 0; q < nstage_max; q++) {
@@ -849,10 +864,12 @@ int batch_build(int precision, const fb_field2d *fields, int nf, int out_f64, fb
             if (q >= plans[f].launches.size())
                 continue;
             const AxisLaunch &a = plans[f].launches[q];
+            const int k = axis_variant_k(precision, a), mode = axis_variant_mode(precision, a);
+            const int sd = a.fill_splat ? 2 : 0;
             Group *g = nullptr;
             for (size_t x = first; x < groups.size(); x++)
-                if (same_launch(groups[x].st.a, a) && same_geometry(groups[x].st.g, plans[f].g) &&
-                    groups[x].st.sv.nbins == plans[f].nbins && groups[x].st.sv.bin_w == plans[f].bin_w)
+                if (groups[x].st.k == k && groups[x].st.mode == mode && groups[x].st.sd == sd &&
+                    groups[x].st.layout == a.layout)
                     g = &groups[x];
             if (!g) {
                 Group ng;
@@ -860,25 +877,38 @@ int batch_build(int precision, const fb_field2d *fields, int nf, int out_f64, fb
                 ng.st.g = plans[f].g;
                 ng.st.sv.nbins = plans[f].nbins;
                 ng.st.sv.bin_w = plans[f].bin_w;
+                ng.st.k = k;
+                ng.st.mode = mode;
+                ng.st.sd = sd;
+                ng.st.layout = a.layout;
                 ng.st.axis = a.axis;
                 ng.q = q;
-                const int64_t grp = a.layout == 0 ? (a.nlines + a.lines_per_cta - 1) / a.lines_per_cta
-                                                  : a.outer_count * a.xblocks;
-                if (grp * a.ntiles > (int64_t)0x7FFFFFFF)
-                    return fail(FB_ERR_ARG, "field %d: too many blocks in one launch", f);
-                ng.st.bpf = (uint32_t)(grp * a.ntiles);
                 groups.push_back(ng);
                 g = &groups.back();
             }
+            const int64_t nb = blocks_of(a);
+            if (nb > (int64_t)0x7FFFFFFF)
+                return fail(FB_ERR_ARG, "field %d: too many blocks in one launch", f);
+            if (!(same_launch(g->st.a, a) && same_geometry(g->st.g, plans[f].g) &&
+                  g->st.sv.nbins == plans[f].nbins && g->st.sv.bin_w == plans[f].bin_w))
+                g->st.mixed = true;
+            g->st.smem = std::max(g->st.smem, axis_smem_bytes(precision, a));
+            g->st.threads = std::max(g->st.threads, axis_threads(precision, a));
             g->f.push_back(f);
+            g->fblocks.push_back((uint32_t)nb);
         }
     }
     for (Group &g : groups) {
-        const int64_t items = (int64_t)g.st.bpf * (int64_t)g.f.size();
-        if (items > (int64_t)0xFFFFFFF0ll)
+        if (kn.mixed)
+            g.st.mixed = true;
+        int64_t items = 0;
+        for (uint32_t nb : g.fblocks)
+            items += nb;
+        if (items > (int64_t)0x7FFFFFFF)
             return fail(FB_ERR_ARG, "batch stage too large");
         g.st.nf = (uint32_t)g.f.size();
         g.st.nitems = (uint32_t)items;
+        g.st.bpf = g.st.mixed ? 0 : g.fblocks[0];
     }
 
     // device layout
@@ -896,7 +926,11 @@ int batch_build(int precision, const fb_field2d *fields, int nf, int out_f64, fb
     off = align_up(off + batch_sort_scratch_bytes(ntot, (uint32_t)nbins, precision));
     for (Group &g : groups) {
         g.st.off_fields = off;
-        off = align_up(off + sizeof(TilePtrs) * g.f.size());
+        off = align_up(off + (g.st.mixed ? sizeof(MixedField) : sizeof(TilePtrs)) * g.f.size());
+        if (g.st.mixed) {
+            g.st.off_items = off;
+            off = align_up(off + sizeof(uint2) * (size_t)g.st.nitems);
+        }
     }
     const size_t tables_end = off;
     std::vector<size_t> pair_off((size_t)nf);
@@ -941,31 +975,71 @@ int batch_build(int precision, const fb_field2d *fields, int nf, int out_f64, fb
                      &recs);
     b->stages.clear();
     for (Group &g : groups) {
-        TilePtrs *tp = reinterpret_cast<TilePtrs *>(img.data() + g.st.off_fields);
-        for (size_t mi = 0; mi < g.f.size(); mi++) {
-            const int f = g.f[mi];
+        auto ptrs = [&](int f) {
             const AxisLaunch &a = plans[f].launches[g.q];
             auto pair = [&](const void *code) -> void * {
                 const int idx = (int)(intptr_t)code - 16;
                 return idx < 0 ? nullptr : dv + pair_off[f] + (size_t)idx * pair_bytes[f];
             };
-            tp[mi].src = pair(a.src_v);
-            tp[mi].dst = pair(a.dst_v);
-            tp[mi].out = fields[f].out;
-            tp[mi].bin_start = reinterpret_cast<const uint32_t *>(dv + b->off_bins) + bin_off[f];
-            tp[mi].hdr = reinterpret_cast<const FieldHeader *>(dv + b->off_hdrs) + f;
-        }
+            TilePtrs t;
+            t.src = pair(a.src_v);
+            t.dst = pair(a.dst_v);
+            t.out = fields[f].out;
+            t.bin_start = reinterpret_cast<const uint32_t *>(dv + b->off_bins) + bin_off[f];
+            t.hdr = reinterpret_cast<const FieldHeader *>(dv + b->off_hdrs) + f;
+            return t;
+        };
+        auto view = [&](int f) {
+            SampleView sv{};
+            sv.rec = recs;
+            sv.npts = ntot;
+            sv.sorted_idx = sorted;
+            sv.nbins = plans[f].nbins;
+            sv.bin_w = plans[f].bin_w;
+            return sv;
+        };
         BatchStage st = g.st;
-        st.a.src_v = st.a.src_w = nullptr;
-        st.a.dst_v = st.a.dst_w = nullptr;
-        st.a.out = nullptr;
-        st.a.out_f64 = b->out_f64;
-        st.sv.rec = recs;
-        st.sv.npts = ntot;
-        st.sv.sorted_idx = sorted;
-        st.sv.bin_start = nullptr;
-        st.sv.hdr = nullptr;
-        e = launch_axis_batch(0, precision, st.a, st.g, st.sv, nullptr, st.bpf, st.nitems, &st.grid, nullptr);
+        if (st.mixed) {
+            MixedField *mf = reinterpret_cast<MixedField *>(img.data() + st.off_fields);
+            for (size_t mi = 0; mi < g.f.size(); mi++) {
+                const int f = g.f[mi];
+                mf[mi].a = plans[f].launches[g.q];
+                mf[mi].a.out_f64 = b->out_f64;
+                mf[mi].g = plans[f].g;
+                mf[mi].sv = view(f);
+                mf[mi].fp = ptrs(f);
+                mf[mi].sv.bin_start = mf[mi].fp.bin_start;
+                mf[mi].sv.hdr = mf[mi].fp.hdr;
+                mf[mi].a.src_v = mf[mi].fp.src;
+                mf[mi].a.dst_v = mf[mi].fp.dst;
+                mf[mi].a.out = mf[mi].fp.out;
+                mf[mi].a.src_w = mf[mi].a.dst_w = nullptr;
+            }
+            // items, the fields with most blocks first
+            std::vector<size_t> order(g.f.size());
+            for (size_t mi = 0; mi < order.size(); mi++)
+                order[mi] = mi;
+            std::stable_sort(order.begin(), order.end(),
+                             [&](size_t x, size_t y) { return g.fblocks[x] > g.fblocks[y]; });
+            uint2 *it = reinterpret_cast<uint2 *>(img.data() + st.off_items);
+            size_t ni = 0;
+            for (size_t mi : order)
+                for (uint32_t bl = 0; bl < g.fblocks[mi]; bl++)
+                    it[ni++] = make_uint2((unsigned)mi, bl);
+            st.grid = (int)st.nitems;
+            e = launch_axis_mixed(0, precision, st.k, st.mode, st.sd, st.layout, nullptr, nullptr, st.nitems,
+                                  st.smem, st.threads, nullptr);
+        } else {
+            TilePtrs *tp = reinterpret_cast<TilePtrs *>(img.data() + st.off_fields);
+            for (size_t mi = 0; mi < g.f.size(); mi++)
+                tp[mi] = ptrs(g.f[mi]);
+            st.a.src_v = st.a.src_w = nullptr;
+            st.a.dst_v = st.a.dst_w = nullptr;
+            st.a.out = nullptr;
+            st.a.out_f64 = b->out_f64;
+            st.sv = view(g.f[0]);
+            e = launch_axis_batch(0, precision, st.a, st.g, st.sv, nullptr, st.bpf, st.nitems, &st.grid, nullptr);
+        }
         if (e != cudaSuccess)
             return cuda_fail(e, "batch axis kernel setup");
         b->stages.push_back(st);
@@ -997,8 +1071,15 @@ int batch_enqueue(fb_batch *b, cudaStream_t st, bool prof)
     }
     for (size_t i = 0; i < b->stages.size(); i++) {
         BatchStage &s = b->stages[i];
-        e = launch_axis_batch(1, b->precision, s.a, s.g, s.sv, reinterpret_cast<const TilePtrs *>(dv + s.off_fields),
-                              s.bpf, s.nitems, &s.grid, st);
+        if (s.mixed)
+            e = launch_axis_mixed(1, b->precision, s.k, s.mode, s.sd, s.layout,
+                                  reinterpret_cast<const MixedField *>(dv + s.off_fields),
+                                  reinterpret_cast<const uint2 *>(dv + s.off_items), s.nitems, s.smem, s.threads,
+                                  st);
+        else
+            e = launch_axis_batch(1, b->precision, s.a, s.g, s.sv,
+                                  reinterpret_cast<const TilePtrs *>(dv + s.off_fields), s.bpf, s.nitems, &s.grid,
+                                  st);
         if (e != cudaSuccess)
             return cuda_fail(e, "batch axis kernel");
         if (prof) {
@@ -1037,6 +1118,7 @@ int batch_tune(int precision, const fb_field2d *fields, int nf, int out_f64, fb_
                 wide = true;
     std::vector<int> chunks = wide ? std::vector<int>{17, 33} : std::vector<int>{0};
     const int rows[3] = {128, 256, 512};
+    const int mixes[2] = {0, 1};
     cudaStream_t st = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
@@ -1045,14 +1127,15 @@ int batch_tune(int precision, const fb_field2d *fields, int nf, int out_f64, fb_
     if (e == cudaSuccess)
         e = cudaEventCreate(&e1);
     float best_ms = 1e30f;
-    *best = fb_batch_knobs{0, 0};
+    *best = fb_batch_knobs{0, 0, 0};
     int rc = e == cudaSuccess ? FB_OK : cuda_fail(e, "tuning stream");
     for (int c : chunks) {
         for (int r : rows) {
+          for (int mx : mixes) {
             if (rc != FB_OK)
                 break;
             fb_batch tb;
-            rc = batch_build(precision, fields, nf, out_f64, fb_batch_knobs{c, r}, &tb);
+            rc = batch_build(precision, fields, nf, out_f64, fb_batch_knobs{c, r, mx}, &tb);
             float t_best = 1e30f;
             for (int it = 0; rc == FB_OK && it < 7; it++) {
                 if (it >= 2)
@@ -1071,10 +1154,11 @@ int batch_tune(int precision, const fb_field2d *fields, int nf, int out_f64, fb_
             }
             if (rc == FB_OK && t_best < best_ms) {
                 best_ms = t_best;
-                *best = fb_batch_knobs{c, r};
+                *best = fb_batch_knobs{c, r, mx};
             }
             cudaStreamSynchronize(st);
             batch_free(&tb);
+          }
         }
     }
     if (e0)
@@ -1099,7 +1183,7 @@ extern "C" int fb_batch_create(int precision, const fb_field2d *fields, int n_fi
         return fail(FB_ERR_ARG, "unknown precision %d", precision);
     if (flags & ~(FB_BATCH_GRAPH | FB_BATCH_TUNE))
         return fail(FB_ERR_ARG, "unknown batch flags 0x%x", flags);
-    fb_batch_knobs kn{0, 0};
+    fb_batch_knobs kn{0, 0, 0};
     if (knobs) {
         kn = *knobs;
     } else if (flags & FB_BATCH_TUNE) {

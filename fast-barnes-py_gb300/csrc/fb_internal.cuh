@@ -174,4 +174,13 @@ struct TilePtrs {
     const FieldHeader *hdr;       // value range of the field
 };
 
+// One field of a mixed batched launch (fields of different grids and
+// parameters sharing one kernel variant), read by the CTA from memory.
+struct MixedField {
+    AxisLaunch a;
+    Geometry g;
+    SampleView sv;
+    TilePtrs fp;
+};
+
 }  // namespace fbg

@@ -42,6 +42,13 @@ cudaError_t launch_axis(int precision, const AxisLaunch &a, const Geometry &g, c
 int axis_threads(int precision, const AxisLaunch &a);
 cudaError_t launch_axis_batch(int op, int precision, const AxisLaunch &a, const Geometry &g, const SampleView &sv,
                               const TilePtrs *fields, uint32_t bpf, uint32_t nitems, int *grid, cudaStream_t st);
+// Mixed batched launches: fields of different shapes sharing the kernel
+// variant (chunk k, mode, splat dimension sd, layout); block x works on
+// items[x] = (field, block).  op 0: set the shared-memory limit; op 1: launch.
+int axis_variant_k(int precision, const AxisLaunch &a);
+int axis_variant_mode(int precision, const AxisLaunch &a);
+cudaError_t launch_axis_mixed(int op, int precision, int k, int mode, int sd, int layout, const MixedField *fields,
+                              const uint2 *items, uint32_t nitems, size_t smem, int threads, cudaStream_t st);
 // Tuning knobs ("chunk": 0 automatic, 17 or 33); returns 0 if accepted.
 int axis_tune(const char *name, int value);
 // Standalone n-pass box filter over contiguous device lines (no splat, no

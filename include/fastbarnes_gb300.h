@@ -114,8 +114,10 @@ int fb_profile_end(int *stages, float *ms, int max_records, int *n_records);
  * demo/timing1_table1_figure4.py:107-115).  A plan holds many independent 2D
  * fields (each its own samples, sigma, grid and output, optimized convolution
  * or convolution) and runs all of them with one sample sort and, per axis
- * stage, one launch for every set of fields of identical grid and parameters.
- * Every field's result equals that of fb_interpolate on it.
+ * stage, one launch per kernel variant (chunk length and pass form): fields
+ * of one shape share a launch description, fields of different grids,
+ * samples and sigma go through a table of per-field descriptions in the same
+ * launch.  Every field's result equals that of fb_interpolate on it.
  *
  * fb_batch_create checks the fields, plans the launches and allocates the
  * plan's device memory (tables, sort scratch, intermediate fields) on the
@@ -145,6 +147,7 @@ typedef struct fb_field2d {
 typedef struct fb_batch_knobs {
     int chunk;                /* 0 automatic, 17 or 33 (float32 windows wider than 65) */
     int rows_threads;         /* x-axis threads per CTA target: 0 (= 256), 128, 256 or 512 */
+    int mixed;                /* 1: per-field descriptions even when the fields share one shape */
 } fb_batch_knobs;
 
 typedef struct fb_batch fb_batch;

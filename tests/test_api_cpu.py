@@ -145,6 +145,9 @@ def test_batch_argument_errors_in_c_abi():
     assert b"chunk" in L.fb_last_error()
     kn = _lib.BatchKnobs(0, 300)
     assert L.fb_batch_create(1, arr, 2, 0, 0, ctypes.byref(kn), ctypes.byref(h)) == _lib.FB_ERR_ARG
+    kn = _lib.BatchKnobs(0, 256, 2)
+    assert L.fb_batch_create(1, arr, 2, 0, 0, ctypes.byref(kn), ctypes.byref(h)) == _lib.FB_ERR_ARG
+    assert b"mixed" in L.fb_last_error()
     arr[1].size[1] = 20   # 2T+1 = 65 >= 20
     assert L.fb_batch_create(1, arr, 2, 0, 0, None, ctypes.byref(h)) == _lib.FB_ERR_KERNEL_SIZE
     assert L.fb_last_error().startswith(b"field 1:")

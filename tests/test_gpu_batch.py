@@ -131,7 +131,7 @@ def test_batch_headline_shape_knobs_and_tuning():
                    step=step, size=size, num_iter=4) for p, v in host]
     refs = [oracle.interpolate(p, v, sigma, x0, step, size, 4, nthreads=8) for p, v in host]
     seen = set()
-    for knobs in ((17, 128), (33, 256), (33, 512), None):
+    for knobs in ((17, 128), (33, 256), (33, 512), (33, 128, 1), None):
         plan = BatchPlan(fields, precision="fp32c", out_dtype=np.float64, graph=True, tune=knobs is None,
                          knobs=knobs)
         got = plan.knobs
@@ -144,3 +144,52 @@ def test_batch_headline_shape_knobs_and_tuning():
         assert launches == 10 and memsets == 2 and nbytes > 0
         plan.close()
     assert len(seen) >= 3
+
+
+def test_many_uneven_fields_one_launch_per_variant():
+    """Forty fields of random grids, sample counts and sigma (some narrow
+    enough for direct sums, some wide): every field equals its single call,
+    and the plan needs one launch per kernel variant and stage."""
+    import torch
+    rng = np.random.default_rng(12)
+    grids = ((96, 64), (256, 128), (300, 200), (512, 256))
+    fields, host = [], []
+    for k in range(40):
+        W, H = grids[rng.integers(len(grids))]
+        N = int(rng.integers(50, 3000))
+        step = 1.0 / 16
+        sigma = float(rng.uniform(0.15, 1.2))
+        n = int(rng.choice([3, 4, 5]))
+        pts = rng.uniform([-0.5, -0.5], [W * step + 0.5, H * step + 0.5], (N, 2))
+        val = 20 * np.cos(pts[:, 0]) + rng.normal(0, 1, N)
+        s = dict(sigma=sigma, x0=(0.0, 0.0), step=step, size=(W, H), n=n, method="optimized_convolution")
+        host.append((pts, val, s))
+        fields.append(dict(pts=torch.as_tensor(pts, device="cuda"), val=torch.as_tensor(val, device="cuda"),
+                           sigma=sigma, x0=(0.0, 0.0), step=step, size=(W, H), num_iter=n))
+    for precision in ("fp32c", "fp64"):
+        plan = BatchPlan(fields, precision=precision, out_dtype=np.float64, graph=True)
+        launches, _, _ = plan.info
+        assert launches <= 8 + 2 * 3, launches   # sort kernels + at most 3 variants per stage
+        outs = [o.cpu().numpy() for o in plan.run()]
+        for (pts, val, s), o in zip(host, outs):
+            ok, msg = same(o, single(pts, val, s, precision))
+            assert ok, (s, msg)
+        plan.close()
+
+
+def test_homogeneous_fields_shared_and_mixed_launches_agree():
+    import torch
+    rng = np.random.default_rng(13)
+    fields = []
+    for b in range(3):
+        pts = rng.uniform(0, [16, 8], (5000, 2))
+        val = rng.normal(0, 1, 5000)
+        fields.append(dict(pts=torch.as_tensor(pts, device="cuda"), val=torch.as_tensor(val, device="cuda"),
+                           sigma=0.5, x0=(0.0, 0.0), step=1 / 32, size=(512, 256), num_iter=4))
+    a = BatchPlan(fields, precision="fp32c", out_dtype=np.float64, knobs=(0, 256, 0))
+    b = BatchPlan(fields, precision="fp32c", out_dtype=np.float64, knobs=(0, 256, 1))
+    oa = [o.cpu().numpy() for o in a.run()]
+    ob = [o.cpu().numpy() for o in b.run()]
+    for x, y in zip(oa, ob):
+        ok, msg = same(x, y)
+        assert ok, msg
