@@ -96,6 +96,8 @@ struct Plan {
     int bin_w = 1;
     std::vector<AxisLaunch> launches;
     int pairs = 0;           // intermediate value/weight field pairs needed
+    bool naive = false;      // method FB_NAIVE: one direct-sum kernel, no launches
+    double sigma[3] = {1, 1, 1};
     // workspace layout
     size_t off_hdr = 0, off_bins = 0, off_sort = 0, off_pair[2] = {0, 0}, total = 0;
 };
@@ -129,7 +131,7 @@ int make_plan(int method, int precision, int dim, int64_t npts, const double *si
         return fail(FB_ERR_ARG, "dim must be 1, 2 or 3 (got %d)", dim);
     if (precision != FB_FP64 && precision != FB_FP32C)
         return fail(FB_ERR_ARG, "unknown precision %d", precision);
-    if (method != FB_OPTIMIZED_CONVOLUTION && method != FB_CONVOLUTION)
+    if (method != FB_OPTIMIZED_CONVOLUTION && method != FB_CONVOLUTION && method != FB_NAIVE)
         return fail(FB_ERR_ARG, "unknown method %d", method);
     if (num_iter < 1)
         return fail(FB_ERR_ARG, "num_iter must be >= 1 (got %d)", num_iter);
@@ -140,6 +142,25 @@ int make_plan(int method, int precision, int dim, int64_t npts, const double *si
     p = Plan();
     p.precision = precision;
     p.npts = npts;
+    if (method == FB_NAIVE) {
+        // interpolation.py:861-938: no kernel size, no mask level; the
+        // workspace holds the value range only
+        p.naive = true;
+        p.g.dim = dim;
+        p.npoints = 1;
+        for (int m = 0; m < 3; m++) {
+            p.g.size[m] = m < dim ? size[m] : 1;
+            p.g.x0[m] = (m < dim && x0) ? x0[m] : 0.0;
+            p.g.step[m] = m < dim ? step[m] : 1.0;
+            p.sigma[m] = m < dim ? sigma[m] : 1.0;
+            if (m < dim && size[m] < 1)
+                return fail(FB_ERR_ARG, "size[%d] must be positive (got %lld)", m, (long long)size[m]);
+            p.npoints *= p.g.size[m];
+        }
+        p.off_hdr = 0;
+        p.total = align_up(sizeof(FieldHeader));
+        return FB_OK;
+    }
     Geometry &g = p.g;
     g.dim = dim;
     g.num_iter = num_iter;
@@ -319,6 +340,141 @@ void resolve_pointers(const Plan &p, char *ws, void *out, AxisLaunch &a)
 
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// adjoint plan: the forward launches storing the final (V, W) cells, the seed,
+// then the same launches again (loading cells instead of splatting) over the
+// seeded gradient cells; routes the cell buffers through the pair slots
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct GradPlan {
+    Plan p;                    // p.launches = forward then adjoint launches
+    size_t nfwd = 0;           // forward launches
+    int seed_pair = 0;         // buffer holding the final cells / the seed
+    int final_pair = 0;        // buffer holding the adjoint cells
+    double thr = 0.0;          // mask level in the units of the stored weights
+};
+
+int make_grad_plan(int method, int precision, int dim, int64_t npts, const double *sigma, const double *x0,
+                   const double *step, const int64_t *size, int num_iter, double max_dist_weight, GradPlan &gp)
+{
+    if (method == FB_NAIVE)
+        return fail(FB_ERR_UNSUPPORTED, "gradients are provided for the convolution methods");
+    int rc = make_plan(method, precision, dim, npts, sigma, x0, step, size, num_iter, max_dist_weight, gp.p);
+    if (rc != FB_OK)
+        return rc;
+    Plan &p = gp.p;
+    std::vector<AxisLaunch> fwd = p.launches;
+    gp.nfwd = fwd.size();
+    gp.thr = fwd.back().thr;
+    std::vector<AxisLaunch> all = fwd;
+    for (AxisLaunch x : fwd) {
+        x.fill_splat = 0;
+        all.push_back(x);
+    }
+    int cur = -1, maxp = 0;
+    for (size_t q = 0; q < all.size(); q++) {
+        AxisLaunch &x = all[q];
+        const bool first = cur == -1;
+        x.store_quot = 0;
+        x.plain = 0;
+        const int src = cur;
+        const int dst = first ? 0 : (x.ntiles == 1 ? src : 1 - src);
+        x.src_v = (const void *)(intptr_t)(src + 16);
+        x.dst_v = (void *)(intptr_t)(dst + 16);
+        maxp = std::max(maxp, dst + 1);
+        cur = dst;
+        if (q + 1 == gp.nfwd)
+            gp.seed_pair = cur;
+    }
+    gp.final_pair = cur;
+    p.launches = all;
+    // cell buffers the forward plan did not need (a 1D forward plan needs
+    // none; tiled adjoint launches may need a second one)
+    const size_t sz = precision == FB_FP64 ? 8 : 4;
+    for (int q = p.pairs; q < maxp; q++) {
+        p.off_pair[q] = p.total;
+        p.total = align_up(p.total + 2 * sz * (size_t)p.npoints);
+    }
+    p.pairs = std::max(p.pairs, maxp);
+    return FB_OK;
+}
+
+}  // namespace
+
+extern "C" int fb_grad_workspace_size(int method, int precision, int dim, int64_t n_pts, const double *sigma,
+                                      const double *step, const int64_t *size, int num_iter, size_t *bytes)
+{
+    GradPlan gp;
+    int rc = make_grad_plan(method, precision, dim, n_pts, sigma, nullptr, step, size, num_iter, 0.0, gp);
+    if (rc != FB_OK)
+        return rc;
+    if (bytes)
+        *bytes = gp.p.total;
+    return FB_OK;
+}
+
+extern "C" int fb_interpolate_grad(int method, int precision, int dim, const double *d_pts, const double *d_val,
+                                   int64_t n_pts, const double *sigma, const double *x0, const double *step,
+                                   const int64_t *size, int num_iter, double max_dist_weight, const void *d_grad_out,
+                                   int grad_f64, double *d_grad_val, double *d_grad_pts, void *d_workspace,
+                                   size_t workspace_bytes, void *stream)
+{
+    g_err[0] = 0;
+    GradPlan gp;
+    int rc = make_grad_plan(method, precision, dim, n_pts, sigma, x0, step, size, num_iter, max_dist_weight, gp);
+    if (rc != FB_OK)
+        return rc;
+    Plan &p = gp.p;
+    if (!x0)
+        return fail(FB_ERR_ARG, "x0 is required");
+    if (!d_grad_out || !d_grad_val || (n_pts > 0 && (!d_pts || !d_val)))
+        return fail(FB_ERR_ARG, "null device pointer");
+    if (!d_workspace || workspace_bytes < p.total)
+        return fail(FB_ERR_WORKSPACE, "workspace of %zu bytes required, %zu given", p.total, workspace_bytes);
+    char *ws = (char *)d_workspace;
+    cudaStream_t st = (cudaStream_t)stream;
+    FieldHeader *hdr = reinterpret_cast<FieldHeader *>(ws + p.off_hdr);
+    uint32_t *bins = reinterpret_cast<uint32_t *>(ws + p.off_bins);
+    uint32_t *scratch = reinterpret_cast<uint32_t *>(ws + p.off_sort);
+    const uint32_t *sorted = nullptr;
+    const void *recs = nullptr;
+    cudaError_t e = sort_samples(p.precision, d_pts, d_val, p.npts, p.g, p.bin_w, p.nbins, hdr, scratch, bins,
+                                 &sorted, &recs, st);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "sample sort");
+    SampleView sv{};
+    sv.rec = recs;
+    sv.npts = p.npts;
+    sv.sorted_idx = sorted;
+    sv.bin_start = bins;
+    sv.nbins = p.nbins;
+    sv.bin_w = p.bin_w;
+    sv.hdr = hdr;
+    const size_t sz = precision == FB_FP64 ? 8 : 4;
+    for (size_t q = 0; q < p.launches.size(); q++) {
+        if (q == gp.nfwd) {
+            e = launch_grad_seed(precision, ws + p.off_pair[gp.seed_pair], p.npoints, d_grad_out, grad_f64, gp.thr,
+                                 st);
+            if (e != cudaSuccess)
+                return cuda_fail(e, "gradient seed");
+        }
+        AxisLaunch a = p.launches[q];
+        resolve_pointers(p, ws, nullptr, a);
+        e = launch_axis(p.precision, a, p.g, sv, st);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "axis kernel");
+    }
+    const uint32_t *keys = nullptr;
+    const void *rec = nullptr;
+    sort_sample_arrays(precision, p.npts, p.nbins, scratch, &keys, &rec);
+    e = launch_grad_gather(precision, dim, rec, keys, p.nbins, p.npts, ws + p.off_pair[gp.final_pair], p.g, hdr,
+                           d_grad_val, d_grad_pts, st);
+    (void)sz;
+    return e == cudaSuccess ? FB_OK : cuda_fail(e, "gradient gather");
+}
+
 extern "C" int fb_workspace_size(int method, int precision, int dim, int64_t n_pts, const double *sigma,
                                  const double *step, const int64_t *size, int num_iter, size_t *bytes)
 {
@@ -395,6 +551,11 @@ extern "C" int fb_profile_end(int *stages, float *ms, int max_records, int *n_re
 static int run_plan(Plan &p, const double *d_pts, const double *d_val, void *d_out, int out_f64, char *ws,
                     cudaStream_t st)
 {
+    if (p.naive) {
+        cudaError_t e = launch_naive(p.precision, p.g.dim, 0, d_pts, d_val, p.npts, p.sigma, p.g.x0, p.g.step,
+                                     p.g.size, reinterpret_cast<FieldHeader *>(ws + p.off_hdr), d_out, out_f64, st);
+        return e == cudaSuccess ? FB_OK : cuda_fail(e, "naive kernel");
+    }
     std::unique_lock<std::mutex> plk(g_prof.mu, std::defer_lock);
     const bool prof = g_prof.on;
     if (prof)
@@ -689,6 +850,27 @@ extern "C" int fb_interpolate_s2(int precision, const double *d_pts, const doubl
     return FB_OK;
 }
 
+extern "C" int fb_interpolate_naive_s2(int precision, const double *d_pts, const double *d_val, int64_t n_pts,
+                                       const double *sigma, const double *x0, const double *step,
+                                       const int64_t *size, void *d_out, int out_f64, void *d_workspace,
+                                       size_t workspace_bytes, void *stream)
+{
+    g_err[0] = 0;
+    if (precision != FB_FP64 && precision != FB_FP32C)
+        return fail(FB_ERR_ARG, "unknown precision %d", precision);
+    if (!sigma || !x0 || !step || !size || size[0] < 1 || size[1] < 1 || n_pts < 0)
+        return fail(FB_ERR_ARG, "invalid naive S2 arguments");
+    if (!d_out || (n_pts > 0 && (!d_pts || !d_val)))
+        return fail(FB_ERR_ARG, "null device pointer");
+    if (!d_workspace || workspace_bytes < sizeof(FieldHeader))
+        return fail(FB_ERR_WORKSPACE, "workspace of %zu bytes required, %zu given", sizeof(FieldHeader),
+                    workspace_bytes);
+    const double sig[2] = {sigma[0], sigma[0]};
+    cudaError_t e = launch_naive(precision, 2, 1, d_pts, d_val, n_pts, sig, x0, step, size,
+                                 reinterpret_cast<FieldHeader *>(d_workspace), d_out, out_f64, (cudaStream_t)stream);
+    return e == cudaSuccess ? FB_OK : cuda_fail(e, "naive S2 kernel");
+}
+
 extern "C" int fb_resample(const float *d_lam, int64_t lam_w, int64_t lam_h, const double *lam_x0, const double *x0,
                            const double *step, const int64_t *size, const double *proj, float *d_out, double *d_tab,
                            void *stream)
@@ -811,6 +993,8 @@ int batch_build(int precision, const fb_field2d *fields, int nf, int out_f64, fb
     std::vector<int64_t> sample_off((size_t)nf), bin_off((size_t)nf);
     for (int f = 0; f < nf; f++) {
         const fb_field2d &F = fields[f];
+        if (F.method == FB_NAIVE)
+            return fail(FB_ERR_UNSUPPORTED, "field %d: batches take the convolution methods", f);
         int rc = make_plan(F.method, precision, 2, F.n_pts, F.sigma, F.x0, F.step, F.size, F.num_iter,
                            F.max_dist_weight, plans[f], kn.chunk, kn.rows_threads);
         if (rc != FB_OK) {

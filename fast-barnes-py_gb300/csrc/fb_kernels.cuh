@@ -56,6 +56,24 @@ int axis_tune(const char *name, int value);
 cudaError_t launch_lines(int precision, void *data, int64_t nlines, int64_t len, int T, double alpha,
                          int passes, int normalize, cudaStream_t st);
 
+// fb_grad.cu: seed (dL/dV, dL/dW) from dL/df in place over the final cells;
+// gather the adjoint cells at every sample's corners.
+cudaError_t launch_grad_seed(int precision, void *cells, int64_t npoints, const void *grad, int grad_f64, double thr,
+                             cudaStream_t st);
+cudaError_t launch_grad_gather(int precision, int dim, const void *rec, const uint32_t *keys, uint32_t skip_key,
+                               int64_t npts, const void *A, const Geometry &g, const FieldHeader *hdr,
+                               double *grad_val, double *grad_pts, cudaStream_t st);
+// fb_sort.cu: the per-sample keys and records (by sample index) that
+// sort_samples leaves in its scratch.
+void sort_sample_arrays(int precision, int64_t npts, uint32_t nbins, uint32_t *scratch, const uint32_t **keys,
+                        const void **rec);
+
+// fb_naive.cu: value range into hdr, then the direct Gaussian sums (sphere:
+// great-circle distances, 2D lon/lat)
+cudaError_t launch_naive(int precision, int dim, int sphere, const double *pts, const double *val, int64_t n,
+                         const double *sigma, const double *x0, const double *step, const int64_t *size,
+                         FieldHeader *hdr, void *out, int out_f64, cudaStream_t st);
+
 // fb_s2.cu
 cudaError_t launch_lambert_to_map(const double *geo, double *map, int64_t n, const double *proj,
                                   cudaStream_t st);

@@ -488,6 +488,14 @@ size_t batch_sort_scratch_bytes(int64_t ntot, uint32_t nbins, int precision)
     return end + 8 * tiles + 256;
 }
 
+void sort_sample_arrays(int precision, int64_t npts, uint32_t nbins, uint32_t *scratch, const uint32_t **keys,
+                        const void **rec)
+{
+    const SortLayout l = sort_layout(scratch, npts, nbins, precision);
+    *keys = l.keys;
+    *rec = l.rec;
+}
+
 void batch_sort_views(int precision, int64_t ntot, uint32_t nbins, uint32_t *scratch, const uint32_t **sorted_idx,
                       const void **recs)
 {

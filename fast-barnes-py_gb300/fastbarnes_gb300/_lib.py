@@ -13,9 +13,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libfastbarnes_gb300.so")
 
 FB_OK = 0
-FB_ERR_ARG, FB_ERR_KERNEL_SIZE = 1, 2
+FB_ERR_ARG, FB_ERR_KERNEL_SIZE, FB_ERR_UNSUPPORTED = 1, 2, 5
 FB_FP64, FB_FP32C = 0, 1
-FB_OPTIMIZED_CONVOLUTION, FB_CONVOLUTION = 0, 1
+FB_OPTIMIZED_CONVOLUTION, FB_CONVOLUTION, FB_NAIVE = 0, 1, 2
 
 PRECISIONS = {"fp64": FB_FP64, "float64": FB_FP64, "fp32c": FB_FP32C}
 
@@ -85,6 +85,8 @@ def lib():
             "fb_workspace_size": ([i, i, i, i64, P, P, P, i, ctypes.POINTER(sz)], i),
             "fb_interpolate": ([i, i, i, P, P, i64, P, P, P, P, i, d, P, i, P, sz, P], i),
             "fb_interpolate_host": ([i, i, i, P, P, i64, P, P, P, P, i, d, P, i, P], i),
+            "fb_grad_workspace_size": ([i, i, i, i64, P, P, P, i, ctypes.POINTER(sz)], i),
+            "fb_interpolate_grad": ([i, i, i, P, P, i64, P, P, P, P, i, d, P, i, P, P, P, sz, P], i),
             "fb_host_alloc": ([sz], P),
             "fb_host_free": ([P], None),
             "fb_release": ([], None),
@@ -94,6 +96,7 @@ def lib():
             "fb_lambert_create_proj": ([d, d, d, d, P], None),
             "fb_lambert_to_map": ([P, P, i64, P, P], i),
             "fb_resample": ([P, i64, i64, P, P, P, P, P, P, P, P], i),
+            "fb_interpolate_naive_s2": ([i, P, P, i64, P, P, P, P, P, i, P, sz, P], i),
             "fb_resample_noalloc": ([P, i64, i64, P, P, P, P, P, P, P], i),
             "fb_tune": ([ctypes.c_char_p, i], i),
             "fb_profile_begin": ([], i),

@@ -17,8 +17,9 @@ Extensions beyond the reference's signature (keyword-only):
 ``pts`` / ``val`` may also be CUDA torch tensors; the result is then a CUDA
 torch tensor and nothing crosses the host.
 
-Methods: 'optimized_convolution' and 'convolution' run on the GPU; 'naive' and
-'radius' are not part of this library and raise NotImplementedError.
+Methods: 'optimized_convolution', 'convolution' and 'naive' (direct Gaussian
+sums, float64 result like the reference's) run on the GPU; 'radius' (kd-tree
+search) is not part of this library and raises NotImplementedError.
 """
 import ctypes
 from math import exp
@@ -220,7 +221,10 @@ def barnes(pts, val, sigma, x0, step, size, method='optimized_convolution', num_
                                + str(sigma))
         raise NotImplementedError("method 'radius' is not provided by fastbarnes_gb300")
     elif method == 'naive':
-        raise NotImplementedError("method 'naive' is not provided by fastbarnes_gb300")
+        # interpolation.py:861-938: no kernel-size check, no max_dist mask,
+        # float64 result like the reference's
+        return _run_grid(_lib.FB_NAIVE, prec, dim, pts, val, sigma, x0, step, size, num_iter, max_dist_weight,
+                         np.float64, tensor_in)
     else:
         raise RuntimeError("encountered invalid Barnes interpolation method: " + method)
 

@@ -7,7 +7,8 @@ Drop-in for ``fastbarnes.interpolationS2`` (MeteoSwiss/fast-barnes-py 2.0):
 pass ``method='optimized_convolution_S2'`` there and here.  The samples are
 projected to the fixed Lambert grid, interpolated there with the optimized
 convolution and resampled to the lon/lat grid, all on the GPU.
-'naive_S2' is not part of this library and raises NotImplementedError.
+'naive_S2' (direct Gaussian sums of great-circle distances, float64 result
+like the reference's) runs on the GPU as well.
 """
 import ctypes
 from math import exp
@@ -57,9 +58,30 @@ def barnes_S2(pts, val, sigma, x0, step, size, method='optimized_convolution', n
         return _run_s2(pts, val, sigma, x0, step, size, num_iter, max_dist_weight, resample,
                        _precision_code(precision))
     elif method == 'naive_S2':
-        raise NotImplementedError("method 'naive_S2' is not provided by fastbarnes_gb300")
+        return _run_naive_s2(pts, val, sigma, x0, step, size, _precision_code(precision))
     else:
         raise RuntimeError("encountered invalid Barnes interpolation method: " + str(method))
+
+
+def _run_naive_s2(pts, val, sigma, x0, step, size, prec):
+    """interpolationS2.py:259-283 on the GPU; float64 result."""
+    torch = _lib.torch_cuda()
+    tensor_in = _is_tensor(pts) or _is_tensor(val)
+    dev = pts.device if _is_tensor(pts) and pts.is_cuda else torch.device("cuda", torch.cuda.current_device())
+    n = int(val.shape[0])
+    if n == 0:
+        raise ValueError('zero-size array to reduction operation minimum which has no identity')
+    tp = torch.as_tensor(pts).to(device=dev, dtype=torch.float64).reshape(n, 2).contiguous()
+    tv = torch.as_tensor(val).to(device=dev, dtype=torch.float64).contiguous()
+    out = torch.empty((int(size[1]), int(size[0])), dtype=torch.float64, device=dev)
+    c_sigma, c_x0, c_step = (_lib.dvec([float(s) for s in a]) for a in (sigma, x0, step))
+    c_size = _lib.dvec([int(s) for s in size], ctypes.c_int64)
+    with torch.cuda.device(dev):
+        ws = _lib.workspace(256, dev)
+        _lib.check(_lib.lib().fb_interpolate_naive_s2(prec, tp.data_ptr(), tv.data_ptr(), n, c_sigma, c_x0, c_step,
+                                                      c_size, out.data_ptr(), 1, ws.data_ptr(), ws.numel(),
+                                                      _lib.stream_ptr(torch, dev)), "fb_interpolate_naive_s2")
+    return out if tensor_in else out.cpu().numpy()
 
 
 def _run_s2(pts, val, sigma, x0, step, size, num_iter, max_dist_weight, resample, prec):

@@ -42,7 +42,8 @@ enum fb_precision {
 
 enum fb_method {
     FB_OPTIMIZED_CONVOLUTION = 0,  /* 'optimized_convolution' (rect kernel + tails) */
-    FB_CONVOLUTION = 1             /* 'convolution' (plain rect kernel)             */
+    FB_CONVOLUTION = 1,            /* 'convolution' (plain rect kernel)             */
+    FB_NAIVE = 2                   /* 'naive' (direct Gaussian sums, O(N x grid))   */
 };
 
 /* Library version string. */
@@ -77,6 +78,10 @@ double fb_sigma_effective(double sigma, double step, int num_iter);
 int fb_workspace_size(int method, int precision, int dim, int64_t n_pts, const double *sigma,
                       const double *step, const int64_t *size, int num_iter, size_t *bytes);
 
+/* FB_NAIVE replaces _interpolate_naive (interpolation.py:861-938): every grid
+ * point sums exp(-|d|^2 / 2 sigma^2) over all samples, NaN only where the
+ * weights sum to zero (no max_dist mask, num_iter and max_dist_weight are
+ * ignored); the float32 form keeps Kahan-compensated float32 sums. */
 int fb_interpolate(int method, int precision, int dim, const double *d_pts, const double *d_val,
                    int64_t n_pts, const double *sigma, const double *x0, const double *step,
                    const int64_t *size, int num_iter, double max_dist_weight, void *d_out, int out_f64,
@@ -91,6 +96,25 @@ int fb_interpolate_host(int method, int precision, int dim, const double *pts, c
                         int64_t n_pts, const double *sigma, const double *x0, const double *step,
                         const int64_t *size, int num_iter, double max_dist_weight, void *out, int out_f64,
                         void *stream);
+
+/* ---- gradients -------------------------------------------------------------
+ * No reference counterpart (the reference has no derivatives).  The adjoint of
+ * fb_interpolate: given dL/df in d_grad_out (same shape as d_out, float32 or
+ * float64 with grad_f64 = 1), writes dL/dval into d_grad_val (n_pts doubles)
+ * and, unless d_grad_pts is NULL, dL/dpts into d_grad_pts (n_pts x dim
+ * doubles).  Masked (NaN) grid points carry no gradient; samples outside the
+ * grid get zero; the value offset (min + max)/2 cancels in f and is treated
+ * as a constant.  The box passes are symmetric, so the adjoint reuses them on
+ * the seeded cells (dL/dV, dL/dW) = (g / W, -g V / W^2) and gathers the
+ * result with the bilinear weights and their position derivatives.  Recomputes
+ * the forward fields; workspace: fb_grad_workspace_size. */
+int fb_grad_workspace_size(int method, int precision, int dim, int64_t n_pts, const double *sigma,
+                           const double *step, const int64_t *size, int num_iter, size_t *bytes);
+int fb_interpolate_grad(int method, int precision, int dim, const double *d_pts, const double *d_val,
+                        int64_t n_pts, const double *sigma, const double *x0, const double *step,
+                        const int64_t *size, int num_iter, double max_dist_weight, const void *d_grad_out,
+                        int grad_f64, double *d_grad_val, double *d_grad_pts, void *d_workspace,
+                        size_t workspace_bytes, void *stream);
 
 /* Pinned host memory for fb_interpolate_host buffers. */
 void *fb_host_alloc(size_t bytes);
@@ -192,6 +216,14 @@ int fb_interpolate_s2(int precision, const double *d_pts, const double *d_val, i
                       const double *sigma, const double *x0, const double *step, const int64_t *size,
                       int num_iter, double max_dist_weight, int resample, float *d_out, void *d_workspace,
                       size_t workspace_bytes, void *stream);
+
+/* Replaces _interpolate_naive_S2 (fastbarnes/interpolationS2.py:259-301):
+ * naive sums of the great-circle distance (degrees) on the lon/lat grid,
+ * sigma[0] in both directions.  d_out: size[1] x size[0]; workspace: 256
+ * bytes. */
+int fb_interpolate_naive_s2(int precision, const double *d_pts, const double *d_val, int64_t n_pts,
+                            const double *sigma, const double *x0, const double *step, const int64_t *size,
+                            void *d_out, int out_f64, void *d_workspace, size_t workspace_bytes, void *stream);
 
 /* Replaces fastbarnes/util/lambert_conformal.py:50-94 (create_proj):
  * proj[5] = {center_lon, n, n_inv, F, rho0}. */

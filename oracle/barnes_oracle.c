@@ -373,6 +373,41 @@ FBO_EXPORT void fbo_interpolate_naive(int dim, const double *pts, const double *
     }
 }
 
+/* fastbarnes/interpolationS2.py:259-301 (_interpolate_naive_S2, _dist_S2):
+ * Gaussian weights of the great-circle distance (degrees) of every sample to
+ * every lon/lat grid point; sigma[0] for both directions. */
+FBO_EXPORT void fbo_interpolate_naive_s2(const double *pts, const double *val, int64_t npts,
+                                         const double *sigma, const double *x0, const double *step,
+                                         const int64_t *size, int nthreads, double *out)
+{
+    double mn = npts > 0 ? val[0] : 0.0, mx = mn;
+    for (int64_t k = 0; k < npts; k++) {
+        if (val[k] < mn) mn = val[k];
+        if (val[k] > mx) mx = val[k];
+    }
+    double offset = (mn + mx) / 2.0;
+    double scale = 2.0 * sigma[0] * sigma[0];
+    int64_t W = size[0], H = size[1];
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 16)
+    for (int64_t g = 0; g < W * H; g++) {
+        int64_t i = g % W, j = g / W;
+        double xc = x0[0] + (double)i * step[0], yc = x0[1] + (double)j * step[1];
+        double lat0 = yc * RAD_PER_DEGREE;
+        double ws = 0.0, wt = 0.0;
+        for (int64_t k = 0; k < npts; k++) {
+            double lat1 = pts[2 * k + 1] * RAD_PER_DEGREE;
+            double arg = sin(lat0) * sin(lat1) + cos(lat0) * cos(lat1) * cos((pts[2 * k] - xc) * RAD_PER_DEGREE);
+            if (arg > 1.0)
+                arg = 1.0;
+            double dist = acos(arg) / RAD_PER_DEGREE;
+            double w = exp(-dist * dist / scale);
+            ws += w * (val[k] - offset);
+            wt += w;
+        }
+        out[g] = wt > 0.0 ? ws / wt + offset : NAN;
+    }
+}
+
 /* ------------------------------------------------------------------------- */
 /* sphere: Lambert conformal projection + resampling                          */
 /* ------------------------------------------------------------------------- */

@@ -55,6 +55,8 @@ def lib():
         L.fbo_interpolate.restype = d
         L.fbo_interpolate_naive.argtypes = [i, P, P, i64, P, P, P, P, i, P]
         L.fbo_interpolate_naive.restype = None
+        L.fbo_interpolate_naive_s2.argtypes = [P, P, i64, P, P, P, P, i, P]
+        L.fbo_interpolate_naive_s2.restype = None
         L.fbo_lambert_create_proj.argtypes = [d, d, d, d, P]
         L.fbo_lambert_to_map.argtypes = [P, P, i64, P]
         L.fbo_resample.argtypes = [P, i64, i64, P, P, P, P, P, P]
@@ -136,6 +138,16 @@ def interpolate_naive(pts, val, sigma, x0, step, size, nthreads=1):
     out = np.empty(tuple(int(s) for s in sz[::-1]), np.float64)
     lib().fbo_interpolate_naive(dim, _p(pts), _p(val), len(val), _p(_vec(sigma, dim)),
                                 _p(_vec(x0, dim)), _p(_vec(step, dim)), _p(sz), int(nthreads), _p(out))
+    return out
+
+
+def interpolate_naive_s2(pts, val, sigma, x0, step, size, nthreads=1):
+    g = np.ascontiguousarray(pts, np.float64)
+    v = np.ascontiguousarray(val, np.float64)
+    sz = _vec(size, 2, np.int64)
+    out = np.empty((int(sz[1]), int(sz[0])), np.float64)
+    lib().fbo_interpolate_naive_s2(_p(g), _p(v), len(v), _p(_vec(sigma, 2)), _p(_vec(x0, 2)), _p(_vec(step, 2)),
+                                   _p(sz), int(nthreads), _p(out))
     return out
 
 

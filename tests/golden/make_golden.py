@@ -14,8 +14,11 @@ Fixtures written (all small, np.savez_compressed):
   barnes_{1,2,3}d.npz - end-to-end barnes() cases: inputs, the float32 result,
                     the float64 quotient before the cast, the NaN threshold
   barnes_s2.npz   - barnes_S2 at step 1/4: Lambert field and resampled field
+  naive.npz       - barnes(method='naive') in 1D/2D/3D and
+                    barnes_S2(method='naive_S2') on small grids
 
 Run once in a container that has the reference; the GPU host never runs it.
+`python make_golden.py naive` regenerates one group of fixtures only.
 """
 import os
 import sys
@@ -197,12 +200,51 @@ def s2_cases(S2):
                         out=out, lam=lam)
 
 
+def naive_cases(I, S2):
+    rng = np.random.default_rng(4242)
+    rec = {}
+    cases = []
+    pts = rng.uniform(-0.1, 3.1, (40, 1))
+    cases.append((pts, rng.normal(5.0, 2.0, 40), 0.2, 0.0, 1 / 64, 200))
+    pts = np.c_[rng.uniform(-0.2, 1.7, 150), rng.uniform(-0.2, 1.3, 150)]
+    cases.append((pts, 1000.0 + 20 * np.sin(pts[:, 0] * 3) + rng.normal(0, 2, 150), (0.3, 0.2), (0.0, 0.0),
+                  1 / 32, (48, 36)))
+    pts = np.c_[rng.uniform(0, 1.5, 60), rng.uniform(0, 1.2, 60), rng.uniform(0, 1.0, 60)]
+    cases.append((pts, rng.normal(0.0, 1.0, 60), 0.25, (0.0, 0.0, 0.0), 1 / 8, (12, 10, 8)))
+    for ci, (pts, val, sigma, x0, step, size) in enumerate(cases):
+        out = I.barnes(pts, val.copy(), sigma, x0, step, size, method="naive")
+        dim = pts.shape[1]
+        rec[f"c{ci}_pts"] = pts
+        rec[f"c{ci}_val"] = val
+        rec[f"c{ci}_sigma"] = np.broadcast_to(np.asarray(sigma, np.float64), (dim,)).copy()
+        rec[f"c{ci}_x0"] = np.broadcast_to(np.asarray(x0, np.float64), (dim,)).copy()
+        rec[f"c{ci}_step"] = np.broadcast_to(np.asarray(step, np.float64), (dim,)).copy()
+        rec[f"c{ci}_size"] = np.broadcast_to(np.asarray(size, np.int64), (dim,)).copy()
+        rec[f"c{ci}_out"] = out
+    rec["count"] = np.int64(len(cases))
+    # sphere: 1-degree grid over part of the European domain
+    pts = np.c_[rng.uniform(-20, 30, 100), rng.uniform(36, 66, 100)]
+    val = 1000.0 + 20 * np.sin(pts[:, 0] / 10) * np.cos(pts[:, 1] / 8) + rng.normal(0, 2, 100)
+    x0, step, size, sigma = np.asarray([-20.0, 36.0]), 1.0, (50, 30), 2.0
+    rec["s2_pts"], rec["s2_val"], rec["s2_x0"] = pts, val, x0
+    rec["s2_step"], rec["s2_size"], rec["s2_sigma"] = np.float64(step), np.array(size), np.float64(sigma)
+    rec["s2_out"] = S2.barnes_S2(pts, val.copy(), sigma, x0, step, size, method="naive_S2")
+    np.savez_compressed(os.path.join(HERE, "naive.npz"), **rec)
+
+
 def main():
     I, S2 = import_reference()
-    accumulation_cases(I)
-    helper_cases(I)
-    barnes_cases(I)
-    s2_cases(S2)
+    which = sys.argv[1:] or ["accumulate", "helpers", "barnes", "s2", "naive"]
+    if "accumulate" in which:
+        accumulation_cases(I)
+    if "helpers" in which:
+        helper_cases(I)
+    if "barnes" in which:
+        barnes_cases(I)
+    if "s2" in which:
+        s2_cases(S2)
+    if "naive" in which:
+        naive_cases(I, S2)
     print("fixtures written to", HERE)
 
 

@@ -169,3 +169,19 @@ def test_resample_noalloc_rejects_grid_beyond_static_scratch():
                                    d([W, H], ctypes.c_int64), proj, 8, None)
         assert rc == _lib.FB_ERR_ARG
         assert b"static scratch" in L.fb_last_error()
+
+
+def test_grad_workspace_holds_cell_fields():
+    """The adjoint keeps the forward's final cells and its own: a 1D forward
+    plan needs no cell buffer, the gradient plan one of 16 B per cell (fp64)."""
+    L = _lib.lib()
+    d = _lib.dvec
+    fwd, grad = ctypes.c_size_t(0), ctypes.c_size_t(0)
+    args = (d([0.3]), d([0.01]), d([5000], ctypes.c_int64), 4)
+    assert L.fb_workspace_size(0, 0, 1, 1000, *args, ctypes.byref(fwd)) == 0
+    assert L.fb_grad_workspace_size(0, 0, 1, 1000, *args, ctypes.byref(grad)) == 0
+    assert grad.value >= fwd.value + 16 * 5000
+    args2 = (d([1.0, 1.0]), d([1 / 32, 1 / 32]), d([400, 300], ctypes.c_int64), 4)
+    assert L.fb_grad_workspace_size(0, 1, 2, 1000, *args2, ctypes.byref(grad)) == 0
+    assert grad.value >= 8 * 400 * 300
+    assert L.fb_grad_workspace_size(2, 0, 2, 1000, *args2, ctypes.byref(grad)) == _lib.FB_ERR_UNSUPPORTED

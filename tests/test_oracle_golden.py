@@ -102,3 +102,23 @@ def test_naive_close_to_optimized():
     inner = (slice(b, -b), slice(b, -b))
     err = np.abs(out[inner] - nv[inner])
     assert np.nanmax(err) < 0.02 * np.ptp(val)
+
+
+def test_oracle_naive_matches_reference(golden):
+    """The naive algorithm: the reference sums with numpy's dot / sum, the
+    oracle sequentially, so the results agree to rounding (1e-12 relative to
+    the value range)."""
+    g = golden("naive.npz")
+    for ci in range(int(g["count"])):
+        args = [g[f"c{ci}_{k}"] for k in ("pts", "val", "sigma", "x0", "step", "size")]
+        ref = g[f"c{ci}_out"]
+        mine = oracle.interpolate_naive(*args)
+        assert np.array_equal(np.isnan(mine), np.isnan(ref))
+        m = ~np.isnan(ref)
+        assert np.max(np.abs(mine[m] - ref[m])) <= 1e-12 * np.ptp(args[1]), ci
+    mine = oracle.interpolate_naive_s2(g["s2_pts"], g["s2_val"], g["s2_sigma"], g["s2_x0"], g["s2_step"],
+                                       g["s2_size"])
+    ref = g["s2_out"]
+    assert np.array_equal(np.isnan(mine), np.isnan(ref))
+    m = ~np.isnan(ref)
+    assert np.max(np.abs(mine[m] - ref[m])) <= 1e-12 * np.ptp(g["s2_val"])
