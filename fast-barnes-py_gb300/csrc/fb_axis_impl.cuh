@@ -318,6 +318,20 @@ __device__ __forceinline__ void clip_chunk(C (&o)[K], int a, int E)
 __device__ __forceinline__ double quotient_div(double v, double w) { return v / w; }
 __device__ __forceinline__ float quotient_div(float v, float w) { return __fdividef(v, w); }
 
+// Drops the `nbits` least significant bits of a float64 mantissa, rounding the
+// kept part the way the reference's demo does (demo/quantization.py:23-37:
+// int(m * 2^(53 - nbits) + 0.5), a truncation toward zero, then
+// ldexp); NaN stays NaN.
+__device__ __forceinline__ double quantize(double x, int nbits)
+{
+    if (nbits <= 0 || x != x)
+        return x;
+    const int sh = 53 - nbits;
+    int e;
+    const double m = frexp(x, &e);
+    return ldexp(trunc(m * ldexp(1.0, sh) + 0.5), e - sh);
+}
+
 template <typename Real>
 __device__ __forceinline__ Real quotient(Real v, Real w, Real thr, Real offset)
 {
@@ -780,7 +794,7 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
                     double *o_ = reinterpret_cast<double *>(fp.out) + gb;
                     for (int e = s0 + tid; e < s1; e += nthr) {
                         const C c = c_[e];
-                        o_[e] = (double)quotient<Real>(c.x, c.y, thr, offs);
+                        o_[e] = quantize((double)quotient<Real>(c.x, c.y, thr, offs), a.quant_bits);
                     }
                 } else {
                     float *o_ = reinterpret_cast<float *>(fp.out) + gb;
@@ -832,7 +846,7 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
 #pragma unroll
                     for (int u = 0; u < HG; u++)
                         if (u0 + u < nl)
-                            o_[u] = (double)q[u];
+                            o_[u] = quantize((double)q[u], a.quant_bits);
                 } else if (q_vec) {
                     *reinterpret_cast<float2 *>(reinterpret_cast<float *>(fp.out) + gi) =
                         make_float2((float)q[0], (float)q[1 % HG]);

@@ -617,6 +617,33 @@ extern "C" int fb_interpolate(int method, int precision, int dim, const double *
     return run_plan(p, d_pts, d_val, d_out, out_f64, (char *)d_workspace, (cudaStream_t)stream);
 }
 
+// Quantised result (demo/quantinterpolation.py:149-153): the float64 quotient
+// with its `quant_bits` least significant mantissa bits dropped in the last
+// axis kernel.
+extern "C" int fb_interpolate_quant(int method, int precision, int dim, const double *d_pts, const double *d_val,
+                                    int64_t n_pts, const double *sigma, const double *x0, const double *step,
+                                    const int64_t *size, int num_iter, double max_dist_weight, int quant_bits,
+                                    double *d_out, void *d_workspace, size_t workspace_bytes, void *stream)
+{
+    g_err[0] = 0;
+    if (quant_bits < 0 || quant_bits > 52)
+        return fail(FB_ERR_ARG, "quant_bits must be in [0, 52] (got %d)", quant_bits);
+    if (method == FB_NAIVE)
+        return fail(FB_ERR_UNSUPPORTED, "quantisation is provided for the convolution methods");
+    Plan p;
+    int rc = make_plan(method, precision, dim, n_pts, sigma, x0, step, size, num_iter, max_dist_weight, p);
+    if (rc != FB_OK)
+        return rc;
+    if (!x0)
+        return fail(FB_ERR_ARG, "x0 is required");
+    if (!d_out || (n_pts > 0 && (!d_pts || !d_val)))
+        return fail(FB_ERR_ARG, "null device pointer");
+    if (!d_workspace || workspace_bytes < p.total)
+        return fail(FB_ERR_WORKSPACE, "workspace of %zu bytes required, %zu given", p.total, workspace_bytes);
+    p.launches.back().quant_bits = quant_bits;
+    return run_plan(p, d_pts, d_val, d_out, 1, (char *)d_workspace, (cudaStream_t)stream);
+}
+
 // ---------------------------------------------------------------------------
 // host-buffer entry
 // ---------------------------------------------------------------------------

@@ -159,6 +159,7 @@ struct AxisLaunch {
     const void *src_v, *src_w;
     void *dst_v, *dst_w;
     void *out;
+    int quant_bits;           // float64 quotient: mantissa bits to drop (0 = none)
     // planning choices (host side only)
     int kchunk;               // chunk length: 0 = automatic, 17 or 33
     int rows_threads;         // rows layout: target threads per CTA (0 = 256)

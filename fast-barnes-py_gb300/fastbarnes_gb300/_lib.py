@@ -85,6 +85,7 @@ def lib():
             "fb_workspace_size": ([i, i, i, i64, P, P, P, i, ctypes.POINTER(sz)], i),
             "fb_interpolate": ([i, i, i, P, P, i64, P, P, P, P, i, d, P, i, P, sz, P], i),
             "fb_interpolate_host": ([i, i, i, P, P, i64, P, P, P, P, i, d, P, i, P], i),
+            "fb_interpolate_quant": ([i, i, i, P, P, i64, P, P, P, P, i, d, i, P, P, sz, P], i),
             "fb_grad_workspace_size": ([i, i, i, i64, P, P, P, i, ctypes.POINTER(sz)], i),
             "fb_interpolate_grad": ([i, i, i, P, P, i64, P, P, P, P, i, d, P, i, P, P, P, sz, P], i),
             "fb_host_alloc": ([sz], P),

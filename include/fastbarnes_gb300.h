@@ -97,6 +97,16 @@ int fb_interpolate_host(int method, int precision, int dim, const double *pts, c
                         const int64_t *size, int num_iter, double max_dist_weight, void *out, int out_f64,
                         void *stream);
 
+/* Replaces demo/quantinterpolation.py:66-155 (barnes with quant_bits): the
+ * float64 result (d_out, size[dim-1] x ... x size[0] doubles) with its
+ * quant_bits least significant mantissa bits dropped as demo/quantization.py
+ * quant() does, applied in the last axis kernel.  quant_bits in [0, 52];
+ * workspace as fb_workspace_size. */
+int fb_interpolate_quant(int method, int precision, int dim, const double *d_pts, const double *d_val,
+                         int64_t n_pts, const double *sigma, const double *x0, const double *step,
+                         const int64_t *size, int num_iter, double max_dist_weight, int quant_bits, double *d_out,
+                         void *d_workspace, size_t workspace_bytes, void *stream);
+
 /* ---- gradients -------------------------------------------------------------
  * No reference counterpart (the reference has no derivatives).  The adjoint of
  * fb_interpolate: given dL/df in d_grad_out (same shape as d_out, float32 or

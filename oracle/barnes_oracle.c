@@ -373,6 +373,24 @@ FBO_EXPORT void fbo_interpolate_naive(int dim, const double *pts, const double *
     }
 }
 
+/* demo/quantization.py:23-37 (quant): drops the nbits least significant bits
+ * of every non-NaN float64, m = frexp mantissa, int(m * 2^(53-nbits) + 0.5)
+ * (a truncation toward zero), ldexp back. */
+FBO_EXPORT void fbo_quant(double *arr, int64_t n, int nbits)
+{
+    if (nbits <= 0)
+        return;
+    int shift = 53 - nbits;
+    for (int64_t i = 0; i < n; i++) {
+        if (arr[i] == arr[i]) {
+            int e;
+            double m = frexp(arr[i], &e);
+            double mi = trunc(m * ldexp(1.0, shift) + 0.5);
+            arr[i] = ldexp(mi, e - shift);
+        }
+    }
+}
+
 /* fastbarnes/interpolationS2.py:259-301 (_interpolate_naive_S2, _dist_S2):
  * Gaussian weights of the great-circle distance (degrees) of every sample to
  * every lon/lat grid point; sigma[0] for both directions. */

@@ -56,6 +56,8 @@ def lib():
         L.fbo_interpolate_naive.argtypes = [i, P, P, i64, P, P, P, P, i, P]
         L.fbo_interpolate_naive.restype = None
         L.fbo_interpolate_naive_s2.argtypes = [P, P, i64, P, P, P, P, i, P]
+        L.fbo_quant.argtypes = [P, i64, i]
+        L.fbo_quant.restype = None
         L.fbo_interpolate_naive_s2.restype = None
         L.fbo_lambert_create_proj.argtypes = [d, d, d, d, P]
         L.fbo_lambert_to_map.argtypes = [P, P, i64, P]
@@ -149,6 +151,13 @@ def interpolate_naive_s2(pts, val, sigma, x0, step, size, nthreads=1):
     lib().fbo_interpolate_naive_s2(_p(g), _p(v), len(v), _p(_vec(sigma, 2)), _p(_vec(x0, 2)), _p(_vec(step, 2)),
                                    _p(sz), int(nthreads), _p(out))
     return out
+
+
+def quant(arr, nbits):
+    """demo/quantization.py quant() on a copy of arr (float64)."""
+    a = np.array(arr, np.float64, copy=True, order="C")
+    lib().fbo_quant(_p(a), a.size, int(nbits))
+    return a
 
 
 def lambert_proj(center_lon=11.5, center_lat=34.5, lat1=42.5, lat2=65.5):

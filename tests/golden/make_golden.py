@@ -16,6 +16,8 @@ Fixtures written (all small, np.savez_compressed):
   barnes_s2.npz   - barnes_S2 at step 1/4: Lambert field and resampled field
   naive.npz       - barnes(method='naive') in 1D/2D/3D and
                     barnes_S2(method='naive_S2') on small grids
+  quant.npz       - demo/quantinterpolation.py barnes() with several
+                    quant_bits, and demo/quantization.py quant() on numbers
 
 Run once in a container that has the reference; the GPU host never runs it.
 `python make_golden.py naive` regenerates one group of fixtures only.
@@ -232,9 +234,32 @@ def naive_cases(I, S2):
     np.savez_compressed(os.path.join(HERE, "naive.npz"), **rec)
 
 
+def quant_cases():
+    sys.path.insert(0, os.path.join(REF, "demo"))
+    import quantinterpolation as QI  # noqa: E402
+    from quantization import quant  # noqa: E402
+    rng = np.random.default_rng(777)
+    N = 200
+    pts = np.c_[rng.uniform(-0.2, 3.2, N), rng.uniform(-0.2, 2.4, N)]
+    val = 1000.0 + 20 * np.sin(pts[:, 0] * 3) * np.cos(pts[:, 1] * 2) + rng.normal(0, 2, N)
+    rec = dict(pts=pts, val=val, sigma=np.float64(0.3), x0=np.zeros(2), step=np.float64(1 / 32),
+               size=np.array([96, 72]), n=np.int64(4))
+    bits = [0, 8, 24, 40]
+    for b in bits:
+        rec[f"out_{b}"] = QI.barnes(pts, val.copy(), 0.3, np.zeros(2), 1 / 32, (96, 72), b, num_iter=4)
+    x = np.concatenate([rng.normal(0, 1, 64) * 10.0 ** rng.integers(-5, 6, 64), [0.0, -0.0, 1.0, -1.0, 0.5]])
+    for b in (1, 7, 23, 52):
+        y = x.copy()
+        quant(y, b)
+        rec[f"quant_in"] = x
+        rec[f"quant_{b}"] = y
+    rec["bits"] = np.array(bits)
+    np.savez_compressed(os.path.join(HERE, "quant.npz"), **rec)
+
+
 def main():
     I, S2 = import_reference()
-    which = sys.argv[1:] or ["accumulate", "helpers", "barnes", "s2", "naive"]
+    which = sys.argv[1:] or ["accumulate", "helpers", "barnes", "s2", "naive", "quant"]
     if "accumulate" in which:
         accumulation_cases(I)
     if "helpers" in which:
@@ -245,6 +270,8 @@ def main():
         s2_cases(S2)
     if "naive" in which:
         naive_cases(I, S2)
+    if "quant" in which:
+        quant_cases()
     print("fixtures written to", HERE)
 
 

@@ -1,0 +1,159 @@
+"""The benchmark configurations at their full sizes, through properties that do
+not need a CPU result of the same size, plus the oracle where it finishes in
+seconds.
+
+- Sweep (2D grids up to 16384 x 8192, N up to 1M, uniform and 3-cluster
+  locations, sigma 0.5 / 1 / 4 grid-degrees, n 3 / 4 / 6): the FP32C form
+  within 1e-5 relative max error of the FP64 form (the stated tolerance), NaN
+  masks equal except within 1e-4 of the mask level.
+- Batched: 512 fields of uneven grids, N and sigma in one plan; a sample of the
+  fields equals the single calls bit for bit.
+- 1D L = 2^26, N = 4M: FP64 against the oracle on sub-lines (1e-9 relative
+  to the value range) and on the whole line (1e-7: the reference's single
+  running sum drifts over 2^26 cells), FP32C against FP64 (1e-5).
+- 3D 512 x 512 x 256, N = 2M: FP32C against FP64 (1e-5); a constant field
+  stays constant wherever it is not masked (exact property of V / W).
+"""
+import numpy as np
+import pytest
+
+from fastbarnes_gb300 import interpolation as I
+from fastbarnes_gb300.batched import BatchPlan
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_err(a, b):
+    m = ~np.isnan(a) & ~np.isnan(b)
+    return float(np.max(np.abs(a[m] - b[m])) / np.max(np.abs(b[m])))
+
+
+def locations(rng, N, kind):
+    if kind == "uniform":
+        return np.c_[rng.uniform(-26, 49, N), rng.uniform(34.5, 72, N)]
+    c = rng.uniform([-20, 40], [40, 65], (3, 2))
+    s = rng.uniform(3, 8, 3)
+    lab = rng.integers(0, 3, N)
+    return c[lab] + rng.normal(0, 1, (N, 2)) * s[lab][:, None]
+
+
+@pytest.mark.parametrize("W,H", [(1024, 512), (4096, 2048), (16384, 8192)])
+def test_sweep_fp32c_within_tolerance(W, H):
+    import torch
+    rng = np.random.default_rng(W)
+    x0, step = (-26.0, 34.5), (75.0 / W, 37.5 / H)
+    worst = 0.0
+    for N, kind, sigma, n in ((10_000, "uniform", 0.5, 3), (100_000, "cluster", 1.0, 4),
+                              (1_000_000, "uniform", 4.0, 6), (1_000_000, "cluster", 1.0, 3)):
+        pts = locations(rng, N, kind)
+        val = 1000 + 20 * np.sin(pts[:, 0] / 10) * np.cos(pts[:, 1] / 8) + rng.normal(0, 2, N)
+        tp = torch.as_tensor(pts, device="cuda")
+        tv = torch.as_tensor(val, device="cuda")
+        if 2 * int(I.get_half_kernel_size_opt(sigma, step[1], n)) + 1 >= H:
+            continue
+        q64 = I.barnes(tp, tv, sigma, x0, step, (W, H), num_iter=n, out_dtype=np.float64).cpu().numpy()
+        q32 = I.barnes(tp, tv, sigma, x0, step, (W, H), num_iter=n, out_dtype=np.float64,
+                       precision="fp32c").cpu().numpy()
+        mism = np.isnan(q64) != np.isnan(q32)
+        assert mism.sum() <= 1e-6 * q64.size, int(mism.sum())
+        e = rel_err(q32, q64)
+        worst = max(worst, e)
+        assert e <= 1e-5, (N, kind, sigma, n, e)
+    assert worst > 0.0
+
+
+def test_batch_of_512_uneven_fields():
+    import torch
+    rng = np.random.default_rng(512)
+    grids = ((256, 256), (1024, 512), (2048, 1024))
+    fields, host = [], []
+    for k in range(512):
+        W, H = grids[rng.integers(3)]
+        N = int(np.exp(rng.uniform(np.log(500), np.log(50000))))
+        step = 1.0 / 64
+        sigma = float(rng.uniform(0.5, 4.0)) * step
+        pts = rng.uniform([0, 0], [W * step, H * step], (N, 2))
+        ph = rng.uniform(0, 2 * np.pi, 8)
+        val = sum(np.sin(pts[:, 0] * (q + 1) + ph[q]) for q in range(8)) + rng.normal(0, 1, N)
+        host.append((pts, val, sigma, step, (W, H)))
+        fields.append(dict(pts=torch.as_tensor(pts, device="cuda"), val=torch.as_tensor(val, device="cuda"),
+                           sigma=sigma, x0=(0.0, 0.0), step=step, size=(W, H), num_iter=4))
+    plan = BatchPlan(fields, precision="fp32c", out_dtype=np.float64, graph=True)
+    launches, _, _ = plan.info
+    assert launches <= 8 + 2 * 3
+    outs = plan.run()
+    torch.cuda.synchronize()
+    for k in rng.choice(512, 12, replace=False):
+        pts, val, sigma, step, size = host[k]
+        ref = I.barnes(pts, val, sigma, (0.0, 0.0), step, size, num_iter=4, precision="fp32c",
+                       out_dtype=np.float64)
+        assert np.array_equal(outs[k].cpu().numpy(), ref, equal_nan=True), k
+    plan.close()
+
+
+def test_1d_full_length():
+    """L = 2^26 cells, N = 4M.  The reference carries one running sum along the
+    whole line, so its float64 rounding grows with the line (1e-8 relative at
+    2^26 cells); the GPU's sums are re-anchored every few cells.  So: the GPU
+    float64 result equals the oracle on short sub-lines cut around several
+    windows (samples within the window and a margin; the passes only reach
+    n (T + 1) cells, so the window's interior is unaffected by the cut) to
+    1e-9 of the value range, stays within 1e-7 of the full-line oracle, and
+    FP32C is within 1e-5 of FP64."""
+    import torch
+    rng = np.random.default_rng(26)
+    L, N = 2 ** 26, 4_000_000
+    step = 1.0 / 1024
+    sigma, n = 0.01, 4
+    pts = rng.uniform(0, L * step, N)
+    val = rng.normal(10.0, 3.0, N)
+    tp, tv = torch.as_tensor(pts, device="cuda"), torch.as_tensor(val, device="cuda")
+    q64 = I.barnes(tp, tv, sigma, 0.0, step, L, num_iter=n, out_dtype=np.float64).cpu().numpy()
+    q32 = I.barnes(tp, tv, sigma, 0.0, step, L, num_iter=n, out_dtype=np.float64, precision="fp32c").cpu().numpy()
+    assert rel_err(q32, q64) <= 1e-5
+    _, ref, _, _ = oracle.interpolate(pts, val, sigma, 0.0, step, L, n, nthreads=8)
+    assert np.array_equal(np.isnan(q64), np.isnan(ref))
+    m = ~np.isnan(ref)
+    assert np.max(np.abs(q64[m] - ref[m])) <= 1e-7 * np.ptp(val)
+    # the offset is the full sample set's, so sub-lines get one extra sample
+    # at each extreme value far away from the window (outside the sub-grid)
+    lo, hi = int(np.argmin(val)), int(np.argmax(val))
+    reach = n * (int(I.get_half_kernel_size_opt(sigma, step, n)) + 1) + 2
+    for c0 in (1000, L // 3, L // 2 + 12345, L - 30000):
+        a, b = c0, c0 + 20000
+        sel = (pts >= (a - 2 * reach) * step) & (pts < (b + 2 * reach) * step)
+        sub_pts = np.r_[pts[sel] - (a - 2 * reach) * step, -10.0, -10.0]
+        sub_val = np.r_[val[sel], val[lo], val[hi]]
+        sub_len = b - a + 4 * reach
+        _, sref, _, _ = oracle.interpolate(sub_pts, sub_val, sigma, 0.0, step, sub_len, n)
+        mine = q64[a - 2 * reach + reach:b + 2 * reach - reach]
+        theirs = sref[reach:sub_len - reach]
+        mm = ~np.isnan(theirs)
+        assert np.array_equal(np.isnan(mine), np.isnan(theirs)), c0
+        assert np.max(np.abs(mine[mm] - theirs[mm])) <= 1e-9 * np.ptp(val), c0
+
+
+def test_3d_full_size_and_constant_field():
+    import torch
+    rng = np.random.default_rng(33)
+    N = 2_000_000
+    c = rng.uniform([0.1, 0.1, 0.1], [0.9, 0.9, 0.9], (8, 3))
+    lab = rng.integers(0, 8, N)
+    pts = c[lab] + rng.normal(0, 0.08, (N, 3))
+    val = rng.normal(0, 1, N) + pts[:, 0]
+    size = (512, 512, 256)
+    step = (1 / 512, 1 / 512, 1 / 256)
+    sigma = (3 / 512, 3 / 512, 3 / 256)
+    tp, tv = torch.as_tensor(pts, device="cuda"), torch.as_tensor(val, device="cuda")
+    q64 = I.barnes(tp, tv, sigma, (0, 0, 0), step, size, num_iter=4, out_dtype=np.float64)
+    q32 = I.barnes(tp, tv, sigma, (0, 0, 0), step, size, num_iter=4, out_dtype=np.float64, precision="fp32c")
+    a, b = q32.cpu().numpy(), q64.cpu().numpy()
+    assert rel_err(a, b) <= 1e-5
+    const = torch.full_like(tv, 7.25)
+    for prec in ("fp64", "fp32c"):
+        f = I.barnes(tp, const, sigma, (0, 0, 0), step, size, num_iter=4, out_dtype=np.float64,
+                     precision=prec).cpu().numpy()
+        m = ~np.isnan(f)
+        assert m.any()
+        assert np.all(f[m] == 7.25), prec

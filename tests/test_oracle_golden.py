@@ -122,3 +122,16 @@ def test_oracle_naive_matches_reference(golden):
     assert np.array_equal(np.isnan(mine), np.isnan(ref))
     m = ~np.isnan(ref)
     assert np.max(np.abs(mine[m] - ref[m])) <= 1e-12 * np.ptp(g["s2_val"])
+
+
+def test_oracle_quant_matches_reference(golden):
+    """demo/quantization.py quant() bit for bit, and the quantised
+    'convolution' result of demo/quantinterpolation.py."""
+    g = golden("quant.npz")
+    for b in (1, 7, 23, 52):
+        assert np.array_equal(oracle.quant(g["quant_in"], b), g[f"quant_{b}"])
+    size = tuple(int(s) for s in g["size"])
+    _, q, _, _ = oracle.interpolate(g["pts"], g["val"], float(g["sigma"]), g["x0"], float(g["step"]), size,
+                                    int(g["n"]), method="convolution")
+    for b in g["bits"]:
+        assert np.array_equal(oracle.quant(q, int(b)), g[f"out_{b}"], equal_nan=True), b
