@@ -980,6 +980,11 @@ struct fb_batch {
     cudaStream_t cap = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    // host-buffer runs: result copies spread over several streams (copy
+    // engines), made at the first fb_batch_run_host
+    static constexpr int kCopyStreams = 4;
+    cudaStream_t copy_st[kCopyStreams] = {};
+    cudaEvent_t copy_ev[kCopyStreams + 1] = {};
 };
 
 namespace {
@@ -992,6 +997,16 @@ void batch_free(fb_batch *b)
         cudaGraphDestroy(b->graph);
     if (b->cap)
         cudaStreamDestroy(b->cap);
+    for (int q = 0; q < fb_batch::kCopyStreams; q++) {
+        if (b->copy_st[q])
+            cudaStreamDestroy(b->copy_st[q]);
+        b->copy_st[q] = nullptr;
+    }
+    for (int q = 0; q <= fb_batch::kCopyStreams; q++) {
+        if (b->copy_ev[q])
+            cudaEventDestroy(b->copy_ev[q]);
+        b->copy_ev[q] = nullptr;
+    }
     if (b->dev)
         cudaFree(b->dev);
     b->exec = nullptr;
@@ -1469,8 +1484,8 @@ extern "C" int fb_batch_run(fb_batch *b, void *stream)
     return FB_OK;
 }
 
-extern "C" int fb_batch_run_host(fb_batch *b, const double *const *h_pts, const double *const *h_val,
-                                 void *const *h_out, void *stream)
+extern "C" int fb_batch_enqueue_host(fb_batch *b, const double *const *h_pts, const double *const *h_val,
+                                     void *const *h_out, void *stream)
 {
     g_err[0] = 0;
     if (!b || !h_pts || !h_val || !h_out)
@@ -1494,19 +1509,52 @@ extern "C" int fb_batch_run_host(fb_batch *b, const double *const *h_pts, const 
     int rc = fb_batch_run(b, stream);
     if (rc != FB_OK)
         return rc;
+    // results back in 16 MiB pieces over several streams, so that several
+    // copy engines share the transfer
+    if (!b->copy_st[0]) {
+        for (int q = 0; q < fb_batch::kCopyStreams && e == cudaSuccess; q++)
+            e = cudaStreamCreateWithFlags(&b->copy_st[q], cudaStreamNonBlocking);
+        for (int q = 0; q <= fb_batch::kCopyStreams && e == cudaSuccess; q++)
+            e = cudaEventCreateWithFlags(&b->copy_ev[q], cudaEventDisableTiming);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "batch copy streams");
+    }
+    e = cudaEventRecord(b->copy_ev[fb_batch::kCopyStreams], st);
+    for (int q = 0; q < fb_batch::kCopyStreams && e == cudaSuccess; q++)
+        e = cudaStreamWaitEvent(b->copy_st[q], b->copy_ev[fb_batch::kCopyStreams], 0);
     const size_t osz = b->out_f64 ? 8 : 4;
+    const size_t piece = (size_t)16 << 20;
+    int next = 0;
     for (int f = 0; f < b->nfields && e == cudaSuccess; f++) {
         const fb_field2d &F = b->fields[f];
         if (!h_out[f])
             return fail(FB_ERR_ARG, "field %d: null host pointer", f);
-        e = cudaMemcpyAsync(h_out[f], F.out, osz * (size_t)F.size[0] * (size_t)F.size[1], cudaMemcpyDeviceToHost,
-                            st);
+        const size_t bytes = osz * (size_t)F.size[0] * (size_t)F.size[1];
+        for (size_t o = 0; o < bytes && e == cudaSuccess; o += piece) {
+            const size_t len = std::min(piece, bytes - o);
+            e = cudaMemcpyAsync((char *)h_out[f] + o, (const char *)F.out + o, len, cudaMemcpyDeviceToHost,
+                                b->copy_st[next]);
+            next = (next + 1) % fb_batch::kCopyStreams;
+        }
     }
-    if (e == cudaSuccess)
-        e = cudaStreamSynchronize(st);
+    for (int q = 0; q < fb_batch::kCopyStreams && e == cudaSuccess; q++) {
+        e = cudaEventRecord(b->copy_ev[q], b->copy_st[q]);
+        if (e == cudaSuccess)
+            e = cudaStreamWaitEvent(st, b->copy_ev[q], 0);
+    }
     if (e != cudaSuccess)
         return cuda_fail(e, "batch results to host");
     return FB_OK;
+}
+
+extern "C" int fb_batch_run_host(fb_batch *b, const double *const *h_pts, const double *const *h_val,
+                                 void *const *h_out, void *stream)
+{
+    int rc = fb_batch_enqueue_host(b, h_pts, h_val, h_out, stream);
+    if (rc != FB_OK)
+        return rc;
+    cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    return e == cudaSuccess ? FB_OK : cuda_fail(e, "batch results to host");
 }
 
 extern "C" int fb_batch_knobs_of(const fb_batch *b, fb_batch_knobs *knobs)

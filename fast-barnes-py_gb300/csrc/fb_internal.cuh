@@ -106,7 +106,7 @@ struct BatchKeyField {
     double x0[2], step[2];
     int64_t size[2];
 };
-constexpr int kBatchKeysPerBlock = 2048;
+constexpr int kBatchKeysPerBlock = 512;
 
 // Sorted-sample view handed to the splatting first-axis kernel.
 struct SampleView {

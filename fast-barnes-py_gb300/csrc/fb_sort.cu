@@ -507,7 +507,7 @@ void batch_sort_views(int precision, int64_t ntot, uint32_t nbins, uint32_t *scr
 static void gather_recs(int precision, const SortLayout &l, const uint32_t *bin_start, uint32_t nbins, int64_t n,
                         cudaStream_t st)
 {
-    const int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
+    const int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)1 << 22);
     if (precision == 0)
         k_gather_recs<double><<<blocks, 256, 0, st>>>(bin_start, nbins, l.sorted,
                                                        reinterpret_cast<const SampleRec<double> *>(l.rec),
@@ -547,7 +547,7 @@ cudaError_t batch_sort(int precision, const BatchKeyField *d_fields, const uint2
     k_scan_exclusive<<<1, 1024, 0, st>>>(l.tsum, toff, (int64_t)tiles);
     k_tile_scan<<<tiles, 1024, 0, st>>>(l.counts, n, toff, bin_start);
     if (ntot > 0) {
-        int blocks = (int)std::min<int64_t>((ntot + 255) / 256, 152 * 8);
+        int blocks = (int)std::min<int64_t>((ntot + 255) / 256, (int64_t)1 << 22);
         k_bin_scatter<<<blocks, 256, 0, st>>>(l.keys, ntot, nbins, bin_start, l.cursor, l.sorted);
         k_sort_bins<<<(unsigned)((nbins + kBinSortWarps - 1) / kBinSortWarps), 32 * kBinSortWarps, 0, st>>>(
             bin_start, nbins, l.sorted, l.large);
@@ -570,7 +570,7 @@ cudaError_t sort_samples(int precision, const double *pts, const double *val, in
     *sorted_idx = l.sorted;
     *recs = l.srec;
     if (npts > 0) {
-        int blocks = (int)std::min<int64_t>((npts + 255) / 256, 152 * 8);
+        int blocks = (int)std::min<int64_t>((npts + 255) / 256, (int64_t)1 << 22);
 #define FBG_KEYS(D, R)                                                                                            \
     k_bin_keys<D, R><<<blocks, 256, 0, st>>>(pts, val, npts, g, bin_w, nbins, l.keys,                              \
                                              reinterpret_cast<SampleRec<R> *>(l.rec), l.counts, hdr)
@@ -593,7 +593,7 @@ cudaError_t sort_samples(int precision, const double *pts, const double *val, in
     }
     k_scan_exclusive<<<1, 1024, 0, st>>>(l.counts, bin_start, (int64_t)nbins + 1);
     if (npts > 0) {
-        int blocks = (int)std::min<int64_t>((npts + 255) / 256, 152 * 8);
+        int blocks = (int)std::min<int64_t>((npts + 255) / 256, (int64_t)1 << 22);
         k_bin_scatter<<<blocks, 256, 0, st>>>(l.keys, npts, nbins, bin_start, l.cursor, l.sorted);
         k_sort_bins<<<(unsigned)((nbins + kBinSortWarps - 1) / kBinSortWarps), 32 * kBinSortWarps, 0, st>>>(
             bin_start, nbins, l.sorted, l.large);

@@ -106,6 +106,7 @@ def lib():
                                  ctypes.POINTER(P)], i),
             "fb_batch_run": ([P, P], i),
             "fb_batch_run_host": ([P, P, P, P, P], i),
+            "fb_batch_enqueue_host": ([P, P, P, P, P], i),
             "fb_batch_knobs_of": ([P, ctypes.POINTER(BatchKnobs)], i),
             "fb_batch_info": ([P, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(sz)], i),
             "fb_batch_destroy": ([P], None),

@@ -198,6 +198,11 @@ int fb_batch_run(fb_batch *plan, void *stream);
  * Pinned host buffers (fb_host_alloc) make the copies asynchronous. */
 int fb_batch_run_host(fb_batch *plan, const double *const *h_pts, const double *const *h_val, void *const *h_out,
                       void *stream);
+/* The same without waiting: everything is enqueued on `stream`, the results
+ * are in h_out once the stream has completed.  With two plans on two streams
+ * a caller overlaps one batch's copies with the other's interpolation. */
+int fb_batch_enqueue_host(fb_batch *plan, const double *const *h_pts, const double *const *h_val,
+                          void *const *h_out, void *stream);
 int fb_batch_knobs_of(const fb_batch *plan, fb_batch_knobs *knobs);
 /* Kernel launches and memsets one fb_batch_run enqueues, and the plan's
  * device bytes. */
