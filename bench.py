@@ -127,9 +127,15 @@ def max_over_ranks(world, x):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cpu" if dist.get_backend() == "gloo" else "cuda"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def field_seed(rank, f):
+    """Seed of field f of a rank's batch: replicas interpolate distinct data."""
+    return 1000 + 97 * rank + f
 
 
 def measured_peak():
@@ -140,6 +146,21 @@ def measured_peak():
         return float(d["hbm_gbs"]), "measured"
     except (OSError, KeyError, ValueError):
         return 6800.0, "fallback"
+
+
+def host_info():
+    """CPU of the machine the baselines run on."""
+    import platform
+    model = None
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu part")):
+                    model = line.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    return {"machine": platform.machine(), "nproc": os.cpu_count(), "model": model}
 
 
 def cpu_oracle_rate(nthreads, seconds=12.0, max_fields=60):
@@ -157,27 +178,40 @@ def cpu_oracle_rate(nthreads, seconds=12.0, max_fields=60):
 
 
 def run_reference(args, world, rank):
-    """--impl reference: the reference's CPU algorithm (oracle port) with all
-    host threads, one field per step."""
+    """--impl reference: the reference's CPU algorithm (the oracle port; the
+    reference's own numba code is not installable here) on all host cores:
+    the reference is sequential, so every core interpolates its own field of
+    the batch, one field per thread per step."""
     if rank != 0:
         return
+    import concurrent.futures as cf
     from oracle import oracle
     oracle.build()
     nth = os.cpu_count() or 1
-    pts, val = field_inputs(1000)
-    for _ in range(args.warmup):
-        oracle.interpolate(pts, val, SIGMA, X0, STEP, (W, H), NITER, MAX_DIST, nthreads=nth)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        oracle.interpolate(pts, val, SIGMA, X0, STEP, (W, H), NITER, MAX_DIST, nthreads=nth)
-    dt = time.perf_counter() - t0
-    value = W * H * args.steps / dt / 1e6
-    sample = f"{args.steps} fields of {W}x{H}, N={NPTS}, float64, one field per step"
+    inputs = [field_inputs(field_seed(0, f)) for f in range(nth)]
+
+    def one(f):
+        pts, val = inputs[f]
+        oracle.interpolate(pts, val, SIGMA, X0, STEP, (W, H), NITER, MAX_DIST, nthreads=1)
+
+    with cf.ThreadPoolExecutor(max_workers=nth) as ex:
+        def step():
+            list(ex.map(one, range(nth)))
+        for _ in range(args.warmup):
+            step()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step()
+        dt = time.perf_counter() - t0
+    value = W * H * nth * args.steps / dt / 1e6
+    sample = (f"{args.steps} steps of {nth} fields of {W}x{H}, N={NPTS}, float64, one field per core "
+              f"(single-threaded each)")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mgridpts/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded)", "config": workload_config(1, "fp64"),
-            "cpu_baseline": {"value": value, "unit": "Mgridpts/s", "cores": nth, "kind": "port", "sample": sample},
+            "data": "synthetic (seeded)", "config": workload_config(nth, "fp64"),
+            "cpu_baseline": {"value": value, "unit": "Mgridpts/s", "cores": nth, "kind": "port", "sample": sample,
+                             "host": host_info()},
             "e2e": {"value": value, "unit": "Mgridpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -218,7 +252,7 @@ def main():
     knobs = tuple(int(x) for x in args.knobs.split(",")) if args.knobs else None
 
     # device-resident inputs, one output per field
-    host = [field_inputs(1000 + 97 * rank + f) for f in range(B)]
+    host = [field_inputs(field_seed(rank, f)) for f in range(B)]
     fields = [dict(pts=torch.as_tensor(p, device=dev), val=torch.as_tensor(v, device=dev), sigma=SIGMA, x0=X0,
                    step=STEP, size=(W, H), num_iter=NITER, max_dist=MAX_DIST) for p, v in host]
     plan = BatchPlan(fields, precision=args.precision, graph=True, tune=knobs is None, knobs=knobs, device=dev)
@@ -430,7 +464,8 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         rate, nf, secs = cpu_oracle_rate(1)
         cpu = {"value": rate, "unit": "Mgridpts/s", "cores": 1, "kind": "port",
-               "sample": f"{nf} field(s) of {W}x{H}, N={NPTS}, float64, single thread, {secs:.1f} s"}
+               "sample": f"{nf} field(s) of {W}x{H}, N={NPTS}, float64, single thread, {secs:.1f} s",
+               "host": host_info()}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "Mgridpts/s", "n_gpus": world, "steps": args.steps,
