@@ -483,6 +483,35 @@ __device__ void apply_recs(C *__restrict__ line, int E, int64_t e0, const StageR
 // the kernel
 // ---------------------------------------------------------------------------
 
+// Stores one thread's final chunk of a column (cells a0 .. a0 + K - 1 of the
+// tile, HBM cell gb + cell * elem_stride), the tile's own cells [s0, s1) only:
+// the quotient (float32 or float64 result) on the last axis, else the cell.
+template <typename Real, typename C, int K>
+__device__ __forceinline__ void store_chunk_columns(const AxisLaunch &a, const TilePtrs &fp, int64_t gb, int a0,
+                                                    int s0, int s1, Real thr, Real offs, const C (&o)[K])
+{
+    const int64_t es = a.elem_stride;
+    if (!a.store_quot) {
+        C *d_ = reinterpret_cast<C *>(fp.dst) + gb;
+#pragma unroll
+        for (int i = 0; i < K; i++)
+            if (a0 + i >= s0 && a0 + i < s1)
+                d_[(int64_t)(a0 + i) * es] = o[i];
+    } else if (a.out_f64) {
+        double *d_ = reinterpret_cast<double *>(fp.out) + gb;
+#pragma unroll
+        for (int i = 0; i < K; i++)
+            if (a0 + i >= s0 && a0 + i < s1)
+                d_[(int64_t)(a0 + i) * es] = (double)quotient<Real>(o[i].x, o[i].y, thr, offs);
+    } else {
+        float *d_ = reinterpret_cast<float *>(fp.out) + gb;
+#pragma unroll
+        for (int i = 0; i < K; i++)
+            if (a0 + i >= s0 && a0 + i < s1)
+                d_[(int64_t)(a0 + i) * es] = (float)quotient<Real>(o[i].x, o[i].y, thr, offs);
+    }
+}
+
 // Column-layout group width: 32 bytes of each grid row.
 template <typename C>
 struct ColG {
@@ -560,6 +589,13 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
     const bool active = li < nl && j < nact;
     const int q = (2 * T + 1) / K, r = (2 * T + 1) - q * K;
     const double offset = (SPLAT_DIM != 0 || a.store_quot) ? field_offset(fp.hdr) : 0.0;
+    const int s0 = (int)(t0 - e0), s1 = (int)(t1 - e0);   // this tile's own cells
+    const Real thr = (Real)a.thr;
+    const Real offs = (Real)offset;
+    // Columns: the last pass stores its outputs from registers (no
+    // write-back, barrier and read of the line buffer).  Loads stay
+    // asynchronous copies: chunk-wise loads into registers were slower.
+    const bool dio = LAYOUT == 1 && SPLAT_DIM == 0 && a.passes > 0 && a.quant_bits <= 0;
 
     // ---- fill -------------------------------------------------------------
     {
@@ -689,6 +725,11 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
                 else
                     direct_dispatch<Real, C, K, ES, 0, false>(T, ln, k0, cu, o);
             }
+            if (dio && pass + 1 == a.passes) {
+                if (active)
+                    store_chunk_columns<Real, C, K>(a, fp, gbase + li, k0, s0, s1, thr, offs, o);
+                break;
+            }
             __syncthreads();
             if (active) {
                 if (k0 + K <= E) {
@@ -760,6 +801,11 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
                         chunk_sums<C, K, false>(o, r, own_s, own_s1, X);
                 }
             }
+            if (dio && !more) {
+                if (active)
+                    store_chunk_columns<Real, C, K>(a, fp, gbase + li, a0, s0, s1, thr, offs, o);
+                break;
+            }
             __syncthreads();
             if (active) {
                 if (a0 >= 0 && a0 + K <= E) {
@@ -779,12 +825,11 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
             }
         }
     }
+    if (dio)
+        return;   // stored from registers by the last pass
     __syncthreads();
 
     // ---- store ------------------------------------------------------------
-    const int s0 = (int)(t0 - e0), s1 = (int)(t1 - e0);   // this tile's own cells
-    const Real thr = (Real)a.thr;
-    const Real offs = (Real)offset;
     if (LAYOUT == 0) {
         for (int q = 0; q < nl; q++) {
             const C *c_ = cells + (size_t)q * P + HP;
@@ -878,16 +923,20 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
     }
 }
 
-// Float32 sliding passes with the short chunk fit in 64 registers, so two
-// 512-thread CTAs (or four of 256) can share an SM; the other variants
-// (long chunk, float64 cells, direct sums) keep 128.
-template <typename Real, int K, int MODE>
-struct AxisMinBlocks {
-    static constexpr int value = (sizeof(Real) == 4 && K == K64 && MODE == 0) ? 2 : 1;
+// Registers per thread (launches have at most 512 threads).  Float32
+// sliding passes with the short chunk fit in 64, so two 512-thread CTAs (or
+// four of 256) can share an SM; with the long chunk, rows fit in 96 without
+// spilling (five 128-thread CTAs an SM instead of four); the other variants
+// (columns with the long chunk, float64 cells, direct sums) keep 128.
+template <typename Real, int K, int MODE, int LAYOUT>
+struct AxisRegs {
+    static constexpr int value = (sizeof(Real) == 4 && MODE == 0 && K == K64)                  ? 64
+                                 : (sizeof(Real) == 4 && MODE == 0 && K == K32 && LAYOUT == 0) ? 96
+                                                                                               : 128;
 };
 
 template <typename Real, int K, int MODE, int SPLAT_DIM, int LAYOUT>
-__global__ void __launch_bounds__(512, AxisMinBlocks<Real, K, MODE>::value)
+__global__ void __maxnreg__((AxisRegs<Real, K, MODE, LAYOUT>::value))
     k_axis(const AxisLaunch a, const Geometry g, const SampleView sv)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -905,7 +954,7 @@ __global__ void __launch_bounds__(512, AxisMinBlocks<Real, K, MODE>::value)
 // description in kernel parameters, one TilePtrs per field); block x of the
 // grid is block x % bpf of field x / bpf.
 template <typename Real, int K, int MODE, int SPLAT_DIM, int LAYOUT>
-__global__ void __launch_bounds__(512, AxisMinBlocks<Real, K, MODE>::value)
+__global__ void __maxnreg__((AxisRegs<Real, K, MODE, LAYOUT>::value))
     k_axis_batch(const AxisLaunch a, const Geometry g, const SampleView sv, const TilePtrs *__restrict__ fields,
                  uint32_t blocks_per_field)
 {
@@ -921,7 +970,7 @@ __global__ void __launch_bounds__(512, AxisMinBlocks<Real, K, MODE>::value)
 // block of that field's launch); the field's description is copied to shared
 // memory first.  Items are ordered largest field first.
 template <typename Real, int K, int MODE, int SPLAT_DIM, int LAYOUT>
-__global__ void __launch_bounds__(512, AxisMinBlocks<Real, K, MODE>::value)
+__global__ void __maxnreg__((AxisRegs<Real, K, MODE, LAYOUT>::value))
     k_axis_mixed(const MixedField *__restrict__ fields, const uint2 *__restrict__ items)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];

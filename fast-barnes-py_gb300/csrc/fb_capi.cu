@@ -898,6 +898,38 @@ extern "C" int fb_interpolate_naive_s2(int precision, const double *d_pts, const
     return e == cudaSuccess ? FB_OK : cuda_fail(e, "naive S2 kernel");
 }
 
+extern "C" int fb_radius_workspace_size(int64_t n_pts, size_t *bytes)
+{
+    g_err[0] = 0;
+    if (!bytes || n_pts < 0)
+        return fail(FB_ERR_ARG, "invalid radius workspace arguments");
+    *bytes = radius_workspace_bytes(n_pts);
+    return FB_OK;
+}
+
+extern "C" int fb_interpolate_radius(int precision, const double *d_pts, const double *d_val, int64_t n_pts,
+                                     double sigma, const double *x0, const double *step, const int64_t *size,
+                                     double max_dist_weight, double min_weight, void *d_out, int out_f64,
+                                     void *d_workspace, size_t workspace_bytes, void *stream)
+{
+    g_err[0] = 0;
+    if (precision != FB_FP64 && precision != FB_FP32C)
+        return fail(FB_ERR_ARG, "unknown precision %d", precision);
+    if (!x0 || !step || !size || size[0] < 1 || size[1] < 1 || n_pts < 0 || !(sigma > 0.0))
+        return fail(FB_ERR_ARG, "invalid radius arguments");
+    if (size[0] > 65535LL * 16 || size[1] > 65535LL * 16)
+        return fail(FB_ERR_KERNEL_SIZE, "radius grid of %lld x %lld points is too large", (long long)size[0],
+                    (long long)size[1]);
+    if (!d_out || (n_pts > 0 && (!d_pts || !d_val)))
+        return fail(FB_ERR_ARG, "null device pointer");
+    const size_t need = radius_workspace_bytes(n_pts);
+    if (!d_workspace || workspace_bytes < need)
+        return fail(FB_ERR_WORKSPACE, "workspace of %zu bytes required, %zu given", need, workspace_bytes);
+    cudaError_t e = launch_radius(precision, d_pts, d_val, n_pts, sigma, x0, step, size, max_dist_weight, min_weight,
+                                  d_workspace, d_out, out_f64, (cudaStream_t)stream);
+    return e == cudaSuccess ? FB_OK : cuda_fail(e, "radius kernel");
+}
+
 extern "C" int fb_resample(const float *d_lam, int64_t lam_w, int64_t lam_h, const double *lam_x0, const double *x0,
                            const double *step, const int64_t *size, const double *proj, float *d_out, double *d_tab,
                            void *stream)

@@ -73,6 +73,12 @@ void sort_sample_arrays(int precision, int64_t npts, uint32_t nbins, uint32_t *s
 cudaError_t launch_naive(int precision, int dim, int sphere, const double *pts, const double *val, int64_t n,
                          const double *sigma, const double *x0, const double *step, const int64_t *size,
                          FieldHeader *hdr, void *out, int out_f64, cudaStream_t st);
+// method 'radius' (2D): value range and sample-tile boxes into the workspace,
+// then the radius-limited sums
+size_t radius_workspace_bytes(int64_t n);
+cudaError_t launch_radius(int precision, const double *pts, const double *val, int64_t n, double sigma,
+                          const double *x0, const double *step, const int64_t *size, double max_dist_weight,
+                          double min_weight, void *ws, void *out, int out_f64, cudaStream_t st);
 
 // fb_s2.cu
 cudaError_t launch_lambert_to_map(const double *geo, double *map, int64_t n, const double *proj,

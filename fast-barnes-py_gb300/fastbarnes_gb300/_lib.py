@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libfastbarnes_gb300.so")
 
 FB_OK = 0
-FB_ERR_ARG, FB_ERR_KERNEL_SIZE, FB_ERR_UNSUPPORTED = 1, 2, 5
+FB_ERR_ARG, FB_ERR_KERNEL_SIZE, FB_ERR_WORKSPACE, FB_ERR_CUDA, FB_ERR_UNSUPPORTED = 1, 2, 3, 4, 5
 FB_FP64, FB_FP32C = 0, 1
 FB_OPTIMIZED_CONVOLUTION, FB_CONVOLUTION, FB_NAIVE = 0, 1, 2
 
@@ -98,6 +98,8 @@ def lib():
             "fb_lambert_to_map": ([P, P, i64, P, P], i),
             "fb_resample": ([P, i64, i64, P, P, P, P, P, P, P, P], i),
             "fb_interpolate_naive_s2": ([i, P, P, i64, P, P, P, P, P, i, P, sz, P], i),
+            "fb_radius_workspace_size": ([i64, ctypes.POINTER(sz)], i),
+            "fb_interpolate_radius": ([i, P, P, i64, d, P, P, P, d, d, P, i, P, sz, P], i),
             "fb_resample_noalloc": ([P, i64, i64, P, P, P, P, P, P, P], i),
             "fb_tune": ([ctypes.c_char_p, i], i),
             "fb_profile_begin": ([], i),

@@ -17,9 +17,11 @@ Extensions beyond the reference's signature (keyword-only):
 ``pts`` / ``val`` may also be CUDA torch tensors; the result is then a CUDA
 torch tensor and nothing crosses the host.
 
-Methods: 'optimized_convolution', 'convolution' and 'naive' (direct Gaussian
-sums, float64 result like the reference's) run on the GPU; 'radius' (kd-tree
-search) is not part of this library and raises NotImplementedError.
+Methods: 'optimized_convolution', 'convolution', 'naive' (direct Gaussian
+sums) and 'radius' (the same sums over the samples within
+sqrt(-2 ln(min_weight)) sigma; the reference's kd-tree search becomes tiles of
+y-sorted samples that a block of grid points skips when out of reach) all run
+on the GPU; 'naive' and 'radius' return float64 like the reference's.
 """
 import ctypes
 from math import exp
@@ -219,7 +221,8 @@ def barnes(pts, val, sigma, x0, step, size, method='optimized_convolution', num_
         if sigma[0] != sigma[1]:
             raise RuntimeError('radius algorithm in 2D works only for scalar sigma value but sigma is: '
                                + str(sigma))
-        raise NotImplementedError("method 'radius' is not provided by fastbarnes_gb300")
+        return _run_radius(prec, pts, val, float(sigma[0]), x0, step, size, max_dist_weight, float(min_weight),
+                           tensor_in)
     elif method == 'naive':
         # interpolation.py:861-938: no kernel-size check, no max_dist mask,
         # float64 result like the reference's
@@ -227,6 +230,38 @@ def barnes(pts, val, sigma, x0, step, size, method='optimized_convolution', num_
                          np.float64, tensor_in)
     else:
         raise RuntimeError("encountered invalid Barnes interpolation method: " + method)
+
+
+def _run_radius(prec, pts, val, sigma, x0, step, size, max_dist_weight, min_weight, tensor_in):
+    """fb_interpolate_radius on the samples sorted by y (a stable device sort,
+    so that the kernel's sample tiles are narrow in y); float64 result."""
+    torch = _lib.torch_cuda()
+    if tensor_in:
+        dev = pts.device if _is_tensor(pts) and pts.is_cuda else torch.device("cuda", torch.cuda.current_device())
+    else:
+        dev = torch.device("cuda", torch.cuda.current_device())
+    npts = int(val.shape[0])
+    tp = torch.as_tensor(pts).to(device=dev, dtype=torch.float64).reshape(npts, 2)
+    tv = torch.as_tensor(val).to(device=dev, dtype=torch.float64)
+    order = torch.argsort(tp[:, 1], stable=True)
+    tp = tp[order].contiguous()
+    tv = tv[order].contiguous()
+    out = torch.empty((int(size[1]), int(size[0])), dtype=torch.float64, device=dev)
+    L = _lib.lib()
+    c_x0 = _lib.dvec([float(s) for s in x0])
+    c_step = _lib.dvec([float(s) for s in step])
+    c_size = _lib.dvec([int(s) for s in size], ctypes.c_int64)
+    need = ctypes.c_size_t(0)
+    with torch.cuda.device(dev):
+        _lib.check(L.fb_radius_workspace_size(npts, ctypes.byref(need)), "fb_radius_workspace_size")
+        ws = _lib.workspace(need.value, dev)
+        rc = L.fb_interpolate_radius(prec, tp.data_ptr(), tv.data_ptr(), npts, sigma, c_x0, c_step, c_size,
+                                     float(max_dist_weight), min_weight, out.data_ptr(), 1, ws.data_ptr(),
+                                     ws.numel(), _lib.stream_ptr(torch, dev))
+        _lib.check(rc, "fb_interpolate_radius")
+    if tensor_in:
+        return out
+    return out.cpu().numpy()
 
 
 # ---------------------------------------------------------------------------

@@ -240,6 +240,20 @@ int fb_interpolate_naive_s2(int precision, const double *d_pts, const double *d_
                             const double *sigma, const double *x0, const double *step, const int64_t *size,
                             void *d_out, int out_f64, void *d_workspace, size_t workspace_bytes, void *stream);
 
+/* Replaces _interpolate_radius (fastbarnes/interpolation.py:809-855) and
+ * its kd-tree search (fastbarnes/util/kdtree.py:208-331): every grid point
+ * sums exp(-d^2 / (2 sigma^2)) over the samples with d^2 <=
+ * (sqrt(-2 ln(min_weight)) sigma)^2, NaN where the weights sum below
+ * max_dist_weight.  2D, one sigma.  The samples may come in any order; sorted
+ * by y (pts[:, 1]) most tiles of samples are out of reach of a block of grid
+ * points and are skipped.  d_out: size[1] x size[0] (float64 for out_f64 = 1,
+ * the reference's type, else float32); workspace: fb_radius_workspace_size(). */
+int fb_radius_workspace_size(int64_t n_pts, size_t *bytes);
+int fb_interpolate_radius(int precision, const double *d_pts, const double *d_val, int64_t n_pts, double sigma,
+                          const double *x0, const double *step, const int64_t *size, double max_dist_weight,
+                          double min_weight, void *d_out, int out_f64, void *d_workspace, size_t workspace_bytes,
+                          void *stream);
+
 /* Replaces fastbarnes/util/lambert_conformal.py:50-94 (create_proj):
  * proj[5] = {center_lon, n, n_inv, F, rho0}. */
 void fb_lambert_create_proj(double center_lon, double center_lat, double lat1, double lat2, double *proj);

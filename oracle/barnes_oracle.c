@@ -373,6 +373,45 @@ FBO_EXPORT void fbo_interpolate_naive(int dim, const double *pts, const double *
     }
 }
 
+/* fastbarnes/interpolation.py:809-855 (_interpolate_radius) with the
+ * kd-tree radius search of fastbarnes/util/kdtree.py:208-331 replaced by a
+ * scan over all samples under the same test: squared distance
+ * (c0 - p0)^2 + (c1 - p1)^2 <= radius^2, radius = sqrt(-2 ln(min_weight))
+ * sigma; weight exp(-d^2 / (2 sigma^2)); NaN where the weights sum below
+ * max_dist_weight.  Sums in sample order (the reference's follow the tree's
+ * order), so this is a tolerance-level oracle.  2D, one sigma. */
+FBO_EXPORT void fbo_interpolate_radius(const double *pts, const double *val, int64_t npts, double sigma,
+                                       const double *x0, const double *step, const int64_t *size,
+                                       double max_dist_weight, double min_weight, int nthreads, double *out)
+{
+    double mn = npts > 0 ? val[0] : 0.0, mx = mn;
+    for (int64_t k = 0; k < npts; k++) {
+        if (val[k] < mn) mn = val[k];
+        if (val[k] > mx) mx = val[k];
+    }
+    const double offset = (mn + mx) / 2.0;
+    const double radius = sqrt(-2.0 * log(min_weight)) * sigma;
+    const double r2 = radius * radius;
+    const double scale = 2.0 * sigma * sigma;
+    const int64_t W = size[0], H = size[1];
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 64)
+    for (int64_t g = 0; g < W * H; g++) {
+        const int64_t i = g % W, j = g / W;
+        const double c0 = x0[0] + (double)i * step[0], c1 = x0[1] + (double)j * step[1];
+        double ws = 0.0, wt = 0.0;
+        for (int64_t k = 0; k < npts; k++) {
+            const double dx = c0 - pts[2 * k], dy = c1 - pts[2 * k + 1];
+            const double d2 = dx * dx + dy * dy;
+            if (d2 <= r2) {
+                const double w = exp(-d2 / scale);
+                ws += w * (val[k] - offset);
+                wt += w;
+            }
+        }
+        out[g] = wt >= max_dist_weight ? ws / wt + offset : NAN;
+    }
+}
+
 /* demo/quantization.py:23-37 (quant): drops the nbits least significant bits
  * of every non-NaN float64, m = frexp mantissa, int(m * 2^(53-nbits) + 0.5)
  * (a truncation toward zero), ldexp back. */

@@ -56,6 +56,8 @@ def lib():
         L.fbo_interpolate_naive.argtypes = [i, P, P, i64, P, P, P, P, i, P]
         L.fbo_interpolate_naive.restype = None
         L.fbo_interpolate_naive_s2.argtypes = [P, P, i64, P, P, P, P, i, P]
+        L.fbo_interpolate_radius.argtypes = [P, P, i64, d, P, P, P, d, d, i, P]
+        L.fbo_interpolate_radius.restype = None
         L.fbo_quant.argtypes = [P, i64, i]
         L.fbo_quant.restype = None
         L.fbo_interpolate_naive_s2.restype = None
@@ -150,6 +152,16 @@ def interpolate_naive_s2(pts, val, sigma, x0, step, size, nthreads=1):
     out = np.empty((int(sz[1]), int(sz[0])), np.float64)
     lib().fbo_interpolate_naive_s2(_p(g), _p(v), len(v), _p(_vec(sigma, 2)), _p(_vec(x0, 2)), _p(_vec(step, 2)),
                                    _p(sz), int(nthreads), _p(out))
+    return out
+
+
+def interpolate_radius(pts, val, sigma, x0, step, size, max_dist=3.5, min_weight=0.001, nthreads=1):
+    g = np.ascontiguousarray(pts, np.float64)
+    v = np.ascontiguousarray(val, np.float64)
+    sz = _vec(size, 2, np.int64)
+    out = np.empty((int(sz[1]), int(sz[0])), np.float64)
+    lib().fbo_interpolate_radius(_p(g), _p(v), len(v), float(sigma), _p(_vec(x0, 2)), _p(_vec(step, 2)), _p(sz),
+                                 math.exp(-max_dist ** 2 / 2), float(min_weight), int(nthreads), _p(out))
     return out
 
 

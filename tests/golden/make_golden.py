@@ -18,6 +18,8 @@ Fixtures written (all small, np.savez_compressed):
                     barnes_S2(method='naive_S2') on small grids
   quant.npz       - demo/quantinterpolation.py barnes() with several
                     quant_bits, and demo/quantization.py quant() on numbers
+  radius.npz      - barnes(method='radius') (kd-tree radius search) on small
+                    2D grids
 
 Run once in a container that has the reference; the GPU host never runs it.
 `python make_golden.py naive` regenerates one group of fixtures only.
@@ -234,6 +236,34 @@ def naive_cases(I, S2):
     np.savez_compressed(os.path.join(HERE, "naive.npz"), **rec)
 
 
+def radius_cases(I):
+    """barnes(method='radius') (kd-tree search) on two small 2D grids: the
+    default min_weight / max_dist, and a larger min_weight with a tighter
+    max_dist so that some grid points are masked."""
+    rng = np.random.default_rng(9090)
+    rec = {}
+    cases = []
+    pts = np.c_[rng.uniform(-0.3, 2.8, 120), rng.uniform(-0.3, 1.9, 120)]
+    val = 1000.0 + 20 * np.sin(pts[:, 0] * 3) * np.cos(pts[:, 1] * 2) + rng.normal(0, 2, 120)
+    cases.append((pts, val, 0.25, (0.0, 0.0), 1 / 16, (40, 28), 3.5, 0.001))
+    pts = np.c_[rng.uniform(0, 3.0, 80), rng.uniform(0, 2.0, 80)]
+    cases.append((pts, rng.normal(5.0, 1.0, 80), 0.15, (0.1, -0.1), (1 / 12, 1 / 10), (36, 24), 2.0, 0.02))
+    for ci, (pts, val, sigma, x0, step, size, max_dist, min_weight) in enumerate(cases):
+        out = I.barnes(pts, val.copy(), sigma, x0, step, size, method="radius", max_dist=max_dist,
+                       min_weight=min_weight)
+        rec[f"c{ci}_pts"] = pts
+        rec[f"c{ci}_val"] = val
+        rec[f"c{ci}_sigma"] = np.float64(sigma)
+        rec[f"c{ci}_x0"] = np.broadcast_to(np.asarray(x0, np.float64), (2,)).copy()
+        rec[f"c{ci}_step"] = np.broadcast_to(np.asarray(step, np.float64), (2,)).copy()
+        rec[f"c{ci}_size"] = np.asarray(size, np.int64)
+        rec[f"c{ci}_max_dist"] = np.float64(max_dist)
+        rec[f"c{ci}_min_weight"] = np.float64(min_weight)
+        rec[f"c{ci}_out"] = out
+    rec["count"] = np.int64(len(cases))
+    np.savez_compressed(os.path.join(HERE, "radius.npz"), **rec)
+
+
 def quant_cases():
     sys.path.insert(0, os.path.join(REF, "demo"))
     import quantinterpolation as QI  # noqa: E402
@@ -259,7 +289,7 @@ def quant_cases():
 
 def main():
     I, S2 = import_reference()
-    which = sys.argv[1:] or ["accumulate", "helpers", "barnes", "s2", "naive", "quant"]
+    which = sys.argv[1:] or ["accumulate", "helpers", "barnes", "s2", "naive", "quant", "radius"]
     if "accumulate" in which:
         accumulation_cases(I)
     if "helpers" in which:
@@ -272,6 +302,8 @@ def main():
         naive_cases(I, S2)
     if "quant" in which:
         quant_cases()
+    if "radius" in which:
+        radius_cases(I)
     print("fixtures written to", HERE)
 
 

@@ -185,3 +185,22 @@ def test_grad_workspace_holds_cell_fields():
     assert L.fb_grad_workspace_size(0, 1, 2, 1000, *args2, ctypes.byref(grad)) == 0
     assert grad.value >= 8 * 400 * 300
     assert L.fb_grad_workspace_size(2, 0, 2, 1000, *args2, ctypes.byref(grad)) == _lib.FB_ERR_UNSUPPORTED
+
+
+def test_radius_entry_checks_before_device_work():
+    """fb_interpolate_radius validates its arguments and workspace on the host
+    (the pointers are never dereferenced here); the workspace holds one
+    32-byte box per tile of 256 samples."""
+    L = _lib.lib()
+    d = _lib.dvec
+    need = ctypes.c_size_t(0)
+    assert L.fb_radius_workspace_size(1000, ctypes.byref(need)) == 0
+    assert need.value >= 4 * 32
+    assert L.fb_radius_workspace_size(-1, ctypes.byref(need)) == _lib.FB_ERR_ARG
+    x0, step, size = d([0.0, 0.0]), d([0.1, 0.1]), d([64, 32], ctypes.c_int64)
+    args = (8, 8, 1000, 0.5, x0, step, size, 0.011, 0.001, 8, 1)
+    assert L.fb_interpolate_radius(0, *args, 8, 16, None) == _lib.FB_ERR_WORKSPACE
+    assert L.fb_interpolate_radius(3, *args, 8, 1 << 20, None) == _lib.FB_ERR_ARG
+    bad = (8, 8, 1000, 0.0, x0, step, size, 0.011, 0.001, 8, 1)
+    assert L.fb_interpolate_radius(0, *bad, 8, 1 << 20, None) == _lib.FB_ERR_ARG
+    assert b"invalid radius arguments" in L.fb_last_error()

@@ -135,3 +135,19 @@ def test_oracle_quant_matches_reference(golden):
                                     int(g["n"]), method="convolution")
     for b in g["bits"]:
         assert np.array_equal(oracle.quant(q, int(b)), g[f"out_{b}"], equal_nan=True), b
+
+
+def test_oracle_radius_matches_reference(golden):
+    """The oracle's radius form (a scan under the kd-tree's distance test)
+    against the reference's barnes(method='radius') on small grids."""
+    g = golden("radius.npz")
+    for ci in range(int(g["count"])):
+        pts, val = g[f"c{ci}_pts"], g[f"c{ci}_val"]
+        mine = oracle.interpolate_radius(pts, val, float(g[f"c{ci}_sigma"]), g[f"c{ci}_x0"], g[f"c{ci}_step"],
+                                         g[f"c{ci}_size"], max_dist=float(g[f"c{ci}_max_dist"]),
+                                         min_weight=float(g[f"c{ci}_min_weight"]))
+        ref = g[f"c{ci}_out"]
+        assert np.array_equal(np.isnan(mine), np.isnan(ref)), ci
+        m = ~np.isnan(ref)
+        assert m.any()
+        assert np.max(np.abs(mine[m] - ref[m])) <= 1e-12 * np.ptp(val), ci
