@@ -307,7 +307,7 @@ def main():
     alg = {0: B * NPTS * (24 + 4 * 6),
            1: B * (NPTS * 28 + W * H * 2 * sz),
            2: B * (W * H * 2 * sz + W * H * 4)}
-    names = {0: "sample sort (7 kernels)", 1: "k_axis_batch x (splat fused)", 2: "k_axis_batch y (quotient fused)"}
+    names = {0: "sample sort (6 kernels)", 1: "k_axis_batch x (splat fused)", 2: "k_axis_batch y (quotient fused)"}
     stage_ms = {k: statistics.median(v) for k, v in per_stage.items()}
     dom = max((k for k in stage_ms if k != 0), key=lambda k: stage_ms[k])
     peak, peak_kind = measured_peak()

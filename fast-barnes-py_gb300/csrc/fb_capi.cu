@@ -1222,6 +1222,7 @@ int batch_build(int precision, const fb_field2d *fields, int nf, int out_f64, fb
         for (int m = 0; m < 2; m++) {
             kf[f].x0[m] = F.x0[m];
             kf[f].step[m] = F.step[m];
+            kf[f].inv_step[m] = 1.0 / F.step[m];
             kf[f].size[m] = F.size[m];
         }
     }
@@ -1602,10 +1603,10 @@ extern "C" int fb_batch_info(const fb_batch *b, int *kernel_launches, int *memse
     if (!b)
         return fail(FB_ERR_ARG, "null plan");
     // batch_sort: k_batch_keys (when there are samples), k_tile_sums,
-    // k_scan_exclusive, k_tile_scan, then k_bin_scatter, k_sort_bins,
-    // k_sort_large, k_gather_recs when there are samples, and two memsets;
-    // then one axis launch per stage with work
-    int k = 3 + (b->nblocks > 0 ? 1 : 0) + (b->ntot > 0 ? 4 : 0);
+    // k_scan_exclusive, k_tile_scan, then k_bin_scatter, k_sort_bins and
+    // k_sort_large (which also put the records in sorted order) when there
+    // are samples, and two memsets; then one axis launch per stage with work
+    int k = 3 + (b->nblocks > 0 ? 1 : 0) + (b->ntot > 0 ? 3 : 0);
     for (const BatchStage &s : b->stages)
         k += s.grid > 0 ? 1 : 0;
     if (kernel_launches)

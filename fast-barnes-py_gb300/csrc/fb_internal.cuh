@@ -64,6 +64,42 @@ __device__ inline double field_offset(const FieldHeader *h)
     return (ordered_to_dbl(~h->vmin_key) + ordered_to_dbl(h->vmax_key)) / 2.0;
 }
 
+// Float32-form cell coordinate t (>= 0 expected) split into the lower cell
+// index and the offset inside the cell with integer operations on the bits of
+// t (float64 instructions are scarce): t = 1.m * 2^e, index = the integer
+// part of the 53-bit mantissa, offset = the 32 leading bits of the rest
+// rounded to float32 (the correctly rounded offset but for ties decided by
+// lower bits).  Returns false (sample skipped) for negative t (but not
+// -0), NaN, infinities and t >= 2^31.
+__device__ __forceinline__ bool split_cell(double t, int &ci, float &cw)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(t);
+    if ((b >> 63) != 0ull)
+        return (b << 1) == 0ull ? (ci = 0, cw = 0.f, true) : false;
+    const int e = (int)(b >> 52) - 1023;   // sign bit is 0
+    if (e >= 31)
+        return false;
+    const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+    if (e < 0) {
+        ci = 0;
+        // t = m * 2^(e - 52); its top 32 bits as an integer, scaled back
+        cw = e < -95 ? 0.f : (float)(uint32_t)(m >> 21) * __int_as_float((e - 31 + 127) << 23);
+        return true;
+    }
+    const int sh = 52 - e;   // fraction bits, 22..52
+    ci = (int)(m >> sh);
+    const unsigned long long fr = m & ((1ull << sh) - 1ull);   // offset * 2^sh
+    if (fr == 0ull) {
+        cw = 0.f;
+        return true;
+    }
+    // the fraction's 32 leading bits (leading one at bit 31), then the scale
+    const int lz = __clzll((long long)fr);
+    const uint32_t top = (uint32_t)((fr << lz) >> 32);
+    cw = (float)top * __int_as_float((32 - lz - sh + 127) << 23);
+    return true;
+}
+
 // Geometry and parameters of one interpolation, shared by all kernels.
 struct Geometry {
     int dim;
@@ -104,6 +140,7 @@ struct BatchKeyField {
     uint32_t bin_offset;     // first global bin (row) of the field
     uint32_t pad;
     double x0[2], step[2];
+    double inv_step[2];      // 1 / step (float32 form: a product instead of a division)
     int64_t size[2];
 };
 constexpr int kBatchKeysPerBlock = 512;

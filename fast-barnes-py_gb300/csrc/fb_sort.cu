@@ -63,14 +63,19 @@ __global__ void k_bin_keys(const double *__restrict__ pts, const double *__restr
                            Geometry g, int bin_w, uint32_t nbins, uint32_t *__restrict__ keys,
                            SampleRec<Real> *__restrict__ rec, uint32_t *__restrict__ counts, FieldHeader *hdr)
 {
+    // float64 instructions kept to the cell coordinates, as in k_batch_keys
     constexpr bool EXACT = sizeof(Real) == 8;
-    const double inv0 = 1.0 / g.step[0], inv1 = 1.0 / g.step[1], inv2 = 1.0 / g.step[2];
+    __shared__ double s_inv[3];
+    if (threadIdx.x < 3)
+        s_inv[threadIdx.x] = 1.0 / g.step[threadIdx.x];
+    __syncthreads();
     unsigned long long kmin = ~0ull, kmax = 0ull;
     int nan = 0;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < npts;
          k += (int64_t)gridDim.x * blockDim.x) {
         const double v = val[k];
-        if (isnan(v)) {
+        const unsigned long long vb = (unsigned long long)__double_as_longlong(v);
+        if ((vb & 0x7fffffffffffffffull) > 0x7ff0000000000000ull) {
             nan = 1;
         } else {
             unsigned long long o = dbl_to_ordered(v);
@@ -79,34 +84,40 @@ __global__ void k_bin_keys(const double *__restrict__ pts, const double *__restr
         }
         uint32_t key = nbins;
         const double *p = pts + k * DIM;
-        const double xc = EXACT ? (p[0] - g.x0[0]) / g.step[0] : (p[0] - g.x0[0]) * inv0;
-        double yc = 0.0, zc = 0.0;
-        bool skip = xc < 0.0 || xc >= (double)(g.size[0] - 1);
-        if (DIM >= 2) {
-            yc = EXACT ? (p[1] - g.x0[1]) / g.step[1] : (p[1] - g.x0[1]) * inv1;
-            skip = skip || yc < 0.0 || yc >= (double)(g.size[1] - 1);
-        }
-        if (DIM == 3) {
-            zc = EXACT ? (p[2] - g.x0[2]) / g.step[2] : (p[2] - g.x0[2]) * inv2;
-            skip = skip || zc < 0.0 || zc >= (double)(g.size[2] - 1);
+        double c[3] = {0.0, 0.0, 0.0};
+        int ci[3] = {0, 0, 0};
+        bool skip = false;
+        Real cw[3] = {0, 0, 0};
+#pragma unroll
+        for (int m = 0; m < DIM; m++) {
+            if (EXACT) {
+                c[m] = (p[m] - g.x0[m]) / g.step[m];
+                ci[m] = __double2int_rz(c[m]);
+                skip = skip || !(c[m] >= 0.0);
+                cw[m] = (Real)(c[m] - (double)ci[m]);
+            } else {
+                float f;
+                skip = skip || !split_cell((p[m] - g.x0[m]) * s_inv[m], ci[m], f);
+                cw[m] = (Real)f;
+            }
+            skip = skip || (int64_t)ci[m] >= g.size[m] - 1;
         }
         SampleRec<Real> r;
         r.xi = r.yi = r.zi = 0;
         r.xw = r.yw = r.zw = 0;
         if (!skip) {
-            const int64_t xi = (int64_t)xc, yi = (int64_t)yc, zi = (int64_t)zc;
-            r.xi = (int32_t)xi;
-            r.yi = (int32_t)yi;
-            r.zi = (int32_t)zi;
-            r.xw = (Real)(xc - (double)xi);
-            r.yw = (Real)(yc - (double)yi);
-            r.zw = (Real)(zc - (double)zi);
+            r.xi = ci[0];
+            r.yi = ci[1];
+            r.zi = ci[2];
+            r.xw = cw[0];
+            r.yw = cw[1];
+            r.zw = cw[2];
             if (DIM == 1)
-                key = (uint32_t)(xi / bin_w);
+                key = (uint32_t)(ci[0] / bin_w);
             else if (DIM == 2)
-                key = (uint32_t)yi;
+                key = (uint32_t)ci[1];
             else
-                key = (uint32_t)(zi * g.size[1] + yi);
+                key = (uint32_t)((int64_t)ci[2] * g.size[1] + ci[1]);
         }
         r.val = v;
         rec[k] = r;
@@ -218,12 +229,24 @@ __device__ __forceinline__ void bitonic(uint32_t *s, int n, int t, int nthr, Syn
     }
 }
 
+// Copies sample record `k` (RW 16-byte words) to position `i` of the sorted
+// record array.
+__device__ __forceinline__ void copy_rec(const uint4 *__restrict__ rec, uint4 *__restrict__ srec, int rw, uint32_t k,
+                                         uint32_t i)
+{
+    for (int w = 0; w < rw; w++)
+        srec[(size_t)i * rw + w] = rec[(size_t)k * rw + w];
+}
+
 // Sorts every bin's entries by sample index: one warp per bin, in registers for
 // up to 32 entries, in shared memory up to kWarpSortMax; larger bins are listed
-// for k_sort_large.
+// for k_sort_large.  Every sorted bin also gets its sample records copied into
+// sorted order (rw 16-byte words a record).
 __global__ void __launch_bounds__(32 * kBinSortWarps) k_sort_bins(const uint32_t *__restrict__ start, uint32_t nbins,
                                                                   uint32_t *__restrict__ sorted,
-                                                                  uint32_t *__restrict__ large)
+                                                                  uint32_t *__restrict__ large,
+                                                                  const uint4 *__restrict__ rec,
+                                                                  uint4 *__restrict__ srec, int rw)
 {
     __shared__ uint32_t buf[kBinSortWarps][kWarpSortMax];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -231,7 +254,7 @@ __global__ void __launch_bounds__(32 * kBinSortWarps) k_sort_bins(const uint32_t
     if (b >= nbins)
         return;
     const uint32_t s0 = start[b], c = start[b + 1] - s0;
-    if (c <= 1)
+    if (c == 0)
         return;
     if (c <= 32) {
         uint32_t x = lane < (int)c ? sorted[s0 + lane] : 0xFFFFFFFFu;
@@ -243,8 +266,10 @@ __global__ void __launch_bounds__(32 * kBinSortWarps) k_sort_bins(const uint32_t
                 x = (lower == asc) ? min(x, y) : max(x, y);
             }
         }
-        if (lane < (int)c)
+        if (lane < (int)c) {
             sorted[s0 + lane] = x;
+            copy_rec(rec, srec, rw, x, s0 + lane);
+        }
         return;
     }
     if (c <= kWarpSortMax) {
@@ -256,8 +281,10 @@ __global__ void __launch_bounds__(32 * kBinSortWarps) k_sort_bins(const uint32_t
             s[i] = i < (int)c ? sorted[s0 + i] : 0xFFFFFFFFu;
         __syncwarp();
         bitonic(s, n, lane, 32, WarpSync());
-        for (int i = lane; i < (int)c; i += 32)
+        for (int i = lane; i < (int)c; i += 32) {
             sorted[s0 + i] = s[i];
+            copy_rec(rec, srec, rw, s[i], s0 + i);
+        }
         return;
     }
     if (lane == 0) {
@@ -268,10 +295,11 @@ __global__ void __launch_bounds__(32 * kBinSortWarps) k_sort_bins(const uint32_t
 
 // Sorts the bins too large for one warp, one block per bin at a time, in a
 // scratch area of twice the bin size (padded to a power of two with keys that
-// sort last).
+// sort last), and copies their records into sorted order.
 __global__ void __launch_bounds__(1024) k_sort_large(const uint32_t *__restrict__ start, uint32_t *__restrict__ sorted,
                                                      const uint32_t *__restrict__ large,
-                                                     uint32_t *__restrict__ scratch)
+                                                     uint32_t *__restrict__ scratch, const uint4 *__restrict__ rec,
+                                                     uint4 *__restrict__ srec, int rw)
 {
     const uint32_t nlarge = large[0];
     for (uint32_t q = blockIdx.x; q < nlarge; q += gridDim.x) {
@@ -285,8 +313,10 @@ __global__ void __launch_bounds__(1024) k_sort_large(const uint32_t *__restrict_
             s[i] = i < (int)c ? sorted[s0 + i] : 0xFFFFFFFFu;
         __syncthreads();
         bitonic(s, n, threadIdx.x, (int)blockDim.x, BlockSync());
-        for (int i = threadIdx.x; i < (int)c; i += blockDim.x)
+        for (int i = threadIdx.x; i < (int)c; i += blockDim.x) {
             sorted[s0 + i] = s[i];
+            copy_rec(rec, srec, rw, s[i], s0 + i);
+        }
         __syncthreads();
     }
 }
@@ -302,16 +332,22 @@ __global__ void k_batch_keys(const BatchKeyField *__restrict__ fields, const uin
                              uint32_t skip_key, uint32_t *__restrict__ keys, SampleRec<Real> *__restrict__ rec,
                              uint32_t *__restrict__ counts, FieldHeader *__restrict__ hdrs)
 {
+    // Float64 instructions are few per SM on this part, so the loop keeps
+    // them to the cell coordinates: the NaN test works on the bits, the
+    // upper bound of the skip rule on the truncated cell index (trunc = floor
+    // for xc >= 0, and xc >= size - 1 <=> floor(xc) >= size - 1; the
+    // conversion saturates), and the float32 form multiplies by 1 / step.
+    // NaN coordinates are skipped.
     constexpr bool EXACT = sizeof(Real) == 8;
     const uint2 bt = blocks[blockIdx.x];   // (field, first sample of the block within the field)
     const BatchKeyField f = fields[bt.x];
-    const double inv0 = 1.0 / f.step[0], inv1 = 1.0 / f.step[1];
     unsigned long long kmin = ~0ull, kmax = 0ull;
     int nan = 0;
     const int64_t end = min(f.npts, (int64_t)bt.y + kBatchKeysPerBlock);
     for (int64_t k = (int64_t)bt.y + threadIdx.x; k < end; k += blockDim.x) {
         const double v = f.val[k];
-        if (isnan(v)) {
+        const unsigned long long vb = (unsigned long long)__double_as_longlong(v);
+        if ((vb & 0x7fffffffffffffffull) > 0x7ff0000000000000ull) {
             nan = 1;
         } else {
             unsigned long long o = dbl_to_ordered(v);
@@ -319,19 +355,33 @@ __global__ void k_batch_keys(const BatchKeyField *__restrict__ fields, const uin
             kmax = o > kmax ? o : kmax;
         }
         const double *p = f.pts + 2 * k;
-        const double xc = EXACT ? (p[0] - f.x0[0]) / f.step[0] : (p[0] - f.x0[0]) * inv0;
-        const double yc = EXACT ? (p[1] - f.x0[1]) / f.step[1] : (p[1] - f.x0[1]) * inv1;
-        const bool skip = xc < 0.0 || yc < 0.0 || xc >= (double)(f.size[0] - 1) || yc >= (double)(f.size[1] - 1);
+        int xi, yi;
+        Real xw, yw;
+        bool skip;
+        if (EXACT) {
+            const double xc = (p[0] - f.x0[0]) / f.step[0], yc = (p[1] - f.x0[1]) / f.step[1];
+            xi = __double2int_rz(xc);
+            yi = __double2int_rz(yc);
+            skip = !(xc >= 0.0) || !(yc >= 0.0);
+            xw = (Real)(xc - (double)xi);
+            yw = (Real)(yc - (double)yi);
+        } else {
+            float xf, yf;
+            skip = !split_cell((p[0] - f.x0[0]) * f.inv_step[0], xi, xf) ||
+                   !split_cell((p[1] - f.x0[1]) * f.inv_step[1], yi, yf);
+            xw = (Real)xf;
+            yw = (Real)yf;
+        }
+        skip = skip || (int64_t)xi >= f.size[0] - 1 || (int64_t)yi >= f.size[1] - 1;
         SampleRec<Real> r;
         r.xi = r.yi = r.zi = 0;
         r.xw = r.yw = r.zw = 0;
         uint32_t key = skip_key;
         if (!skip) {
-            const int64_t xi = (int64_t)xc, yi = (int64_t)yc;
-            r.xi = (int32_t)xi;
-            r.yi = (int32_t)yi;
-            r.xw = (Real)(xc - (double)xi);
-            r.yw = (Real)(yc - (double)yi);
+            r.xi = xi;
+            r.yi = yi;
+            r.xw = xw;
+            r.yw = yw;
             key = f.bin_offset + (uint32_t)yi;
         }
         r.val = v;
@@ -417,17 +467,6 @@ __global__ void __launch_bounds__(1024) k_tile_scan(const uint32_t *__restrict__
     }
 }
 
-// Records in sorted order: the splat then reads each line's records as one
-// contiguous run instead of gathering them through the index list.
-template <typename Real>
-__global__ void k_gather_recs(const uint32_t *__restrict__ bin_start, uint32_t nbins,
-                              const uint32_t *__restrict__ sorted, const SampleRec<Real> *__restrict__ rec,
-                              SampleRec<Real> *__restrict__ out)
-{
-    const uint32_t total = bin_start[nbins];
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x)
-        out[i] = rec[sorted[i]];
-}
 
 // Scratch layout: counts[nbins + 2] | cursor[nbins + 2] | large[nbins + 2] |
 // keys[N] | sorted[N] | big-bin scratch[2N] (uint32), then the sample records
@@ -441,6 +480,8 @@ struct SortLayout {
 };
 
 size_t rec_bytes(int precision) { return precision == 0 ? sizeof(SampleRec<double>) : sizeof(SampleRec<float>); }
+static_assert(sizeof(SampleRec<double>) % 16 == 0 && sizeof(SampleRec<float>) % 16 == 0,
+              "records are copied as 16-byte words");
 size_t up256(size_t x) { return (x + 255) / 256 * 256; }
 
 // Byte offsets of the record arrays and of the end of the sorted records.
@@ -504,19 +545,6 @@ void batch_sort_views(int precision, int64_t ntot, uint32_t nbins, uint32_t *scr
     *recs = l.srec;
 }
 
-static void gather_recs(int precision, const SortLayout &l, const uint32_t *bin_start, uint32_t nbins, int64_t n,
-                        cudaStream_t st)
-{
-    const int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)1 << 22);
-    if (precision == 0)
-        k_gather_recs<double><<<blocks, 256, 0, st>>>(bin_start, nbins, l.sorted,
-                                                       reinterpret_cast<const SampleRec<double> *>(l.rec),
-                                                       reinterpret_cast<SampleRec<double> *>(l.srec));
-    else
-        k_gather_recs<float><<<blocks, 256, 0, st>>>(bin_start, nbins, l.sorted,
-                                                      reinterpret_cast<const SampleRec<float> *>(l.rec),
-                                                      reinterpret_cast<SampleRec<float> *>(l.srec));
-}
 
 cudaError_t batch_sort(int precision, const BatchKeyField *d_fields, const uint2 *d_blocks, uint32_t nblocks,
                        int64_t ntot, uint32_t nbins, FieldHeader *hdrs, int nfields, uint32_t *scratch,
@@ -549,10 +577,12 @@ cudaError_t batch_sort(int precision, const BatchKeyField *d_fields, const uint2
     if (ntot > 0) {
         int blocks = (int)std::min<int64_t>((ntot + 255) / 256, (int64_t)1 << 22);
         k_bin_scatter<<<blocks, 256, 0, st>>>(l.keys, ntot, nbins, bin_start, l.cursor, l.sorted);
+        const int rw = (int)(rec_bytes(precision) / 16);
+        const uint4 *rec4 = reinterpret_cast<const uint4 *>(l.rec);
+        uint4 *srec4 = reinterpret_cast<uint4 *>(l.srec);
         k_sort_bins<<<(unsigned)((nbins + kBinSortWarps - 1) / kBinSortWarps), 32 * kBinSortWarps, 0, st>>>(
-            bin_start, nbins, l.sorted, l.large);
-        k_sort_large<<<64, 1024, 0, st>>>(bin_start, l.sorted, l.large, l.big);
-        gather_recs(precision, l, bin_start, nbins, ntot, st);
+            bin_start, nbins, l.sorted, l.large, rec4, srec4, rw);
+        k_sort_large<<<64, 1024, 0, st>>>(bin_start, l.sorted, l.large, l.big, rec4, srec4, rw);
     }
     return cudaGetLastError();
 }
@@ -595,10 +625,12 @@ cudaError_t sort_samples(int precision, const double *pts, const double *val, in
     if (npts > 0) {
         int blocks = (int)std::min<int64_t>((npts + 255) / 256, (int64_t)1 << 22);
         k_bin_scatter<<<blocks, 256, 0, st>>>(l.keys, npts, nbins, bin_start, l.cursor, l.sorted);
+        const int rw = (int)(rec_bytes(precision) / 16);
+        const uint4 *rec4 = reinterpret_cast<const uint4 *>(l.rec);
+        uint4 *srec4 = reinterpret_cast<uint4 *>(l.srec);
         k_sort_bins<<<(unsigned)((nbins + kBinSortWarps - 1) / kBinSortWarps), 32 * kBinSortWarps, 0, st>>>(
-            bin_start, nbins, l.sorted, l.large);
-        k_sort_large<<<64, 1024, 0, st>>>(bin_start, l.sorted, l.large, l.big);
-        gather_recs(precision, l, bin_start, nbins, npts, st);
+            bin_start, nbins, l.sorted, l.large, rec4, srec4, rw);
+        k_sort_large<<<64, 1024, 0, st>>>(bin_start, l.sorted, l.large, l.big, rec4, srec4, rw);
     }
     return cudaGetLastError();
 }
