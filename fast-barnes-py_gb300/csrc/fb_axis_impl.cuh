@@ -98,6 +98,15 @@ template <>
 __device__ __forceinline__ float2 csplat<float2>(double x) { return make_float2((float)x, (float)x); }
 template <>
 __device__ __forceinline__ double2 csplat<double2>(double x) { return make_double2(x, x); }
+// both halves from a value already in the cell's precision
+template <typename C>
+__device__ __forceinline__ C cpair(float x);
+template <typename C>
+__device__ __forceinline__ C cpair(double x);
+template <>
+__device__ __forceinline__ float2 cpair<float2>(float x) { return make_float2(x, x); }
+template <>
+__device__ __forceinline__ double2 cpair<double2>(double x) { return make_double2(x, x); }
 
 // 16-byte asynchronous global -> shared copies (no registers held while the
 // data is in flight, so a thread can have all of its copies outstanding)
@@ -588,10 +597,25 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
     const int nact = MODE == 1 ? nch : (E + T + 1 + K - 1) / K;
     const bool active = li < nl && j < nact;
     const int q = (2 * T + 1) / K, r = (2 * T + 1) - q * K;
-    const double offset = (SPLAT_DIM != 0 || a.store_quot) ? field_offset(fp.hdr) : 0.0;
+    // The field's offset and the float32 form's scalar parameters are
+    // computed once per CTA: float64 instructions (including conversions to
+    // float32) are scarce, and every thread needs them.
+    __shared__ double s_offset;
+    __shared__ Real s_par[5];   // alpha, alpha * inv_norm, inv_norm, thr, offset in the form's precision
+    if (tid == 0) {
+        const double off = (SPLAT_DIM != 0 || a.store_quot) ? field_offset(fp.hdr) : 0.0;
+        s_offset = off;
+        s_par[0] = (Real)a.alpha;
+        s_par[1] = (Real)(a.alpha * a.inv_norm);
+        s_par[2] = (Real)a.inv_norm;
+        s_par[3] = (Real)a.thr;
+        s_par[4] = (Real)off;
+    }
+    __syncthreads();
+    const double offset = s_offset;
     const int s0 = (int)(t0 - e0), s1 = (int)(t1 - e0);   // this tile's own cells
-    const Real thr = (Real)a.thr;
-    const Real offs = (Real)offset;
+    const Real thr = s_par[3];
+    const Real offs = s_par[4];
     // Columns: the last pass stores its outputs from registers (no
     // write-back, barrier and read of the line buffer).  Loads stay
     // asynchronous copies: chunk-wise loads into registers were slower.
@@ -707,11 +731,11 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
 
     // ---- passes -----------------------------------------------------------
     PassCoef<C, false> cu;
-    cu.alpha = csplat<C>(a.alpha);
-    cu.inv = csplat<C>(1.0);
+    cu.alpha = cpair<C>(s_par[0]);
+    cu.inv = cpair<C>((Real)1);
     PassCoef<C, true> cs;
-    cs.alpha = csplat<C>(a.alpha * a.inv_norm);
-    cs.inv = csplat<C>(a.inv_norm);
+    cs.alpha = cpair<C>(s_par[1]);
+    cs.inv = cpair<C>(s_par[2]);
 
     if constexpr (MODE == 1) {
         // direct sums, F grid every pass
