@@ -454,6 +454,21 @@ def main():
            for q in range(2)]
     ref0 = plan.outs[0].cpu().numpy()
     e2e_ok = all(bool(np.array_equal(c, ref0, equal_nan=True)) for c in chk)
+    # the host link alone: the same float32 result bytes device -> pinned
+    # host by the copy engine (the e2e form cannot beat this transfer)
+    dev_res = torch.empty(B * W * H, dtype=torch.float32, device=dev)
+    pin_res = torch.empty(B * W * H, dtype=torch.float32, pin_memory=True)
+    with torch.cuda.stream(streams[0]):
+        pin_res.copy_(dev_res, non_blocking=True)
+        e0_, e1_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0_.record()
+        for _ in range(3):
+            pin_res.copy_(dev_res, non_blocking=True)
+        e1_.record()
+    e1_.synchronize()
+    link_gbs = 3 * B * W * H * 4 / (e0_.elapsed_time(e1_) * 1e-3) / 1e9
+    link_bound = W * H * B / (B * W * H * 4 / (link_gbs * 1e9)) / 1e6
+    del dev_res, pin_res
     for p in h_pts + h_val + h_out[0] + h_out[1]:
         L.fb_host_free(p)
     plan.close()
@@ -492,6 +507,8 @@ def main():
                                      "stage_ms_per_field": single_stage_ms},
                 "e2e": {"value": e2e_value, "unit": "Mgridpts/s", "h2d_bytes_per_step": B * NPTS * 24,
                         "d2h_bytes_per_step": B * W * H * 4, "matches_device_result": e2e_ok,
+                        "link_d2h_gbs": link_gbs, "link_bound_value": link_bound,
+                        "frac_of_link_bound": e2e_value / link_bound,
                         "entry": "fb_batch_enqueue_host (pinned host buffers; two plans on two streams, "
                                  "each step's copies overlap the next step's interpolation)"},
                 "cpu_baseline": cpu, "clocks": clk.summary(),
