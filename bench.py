@@ -382,6 +382,24 @@ def main():
     e1.record(stream)
     torch.cuda.synchronize()
     fp64_value = W * H * B * k64 / (e0.elapsed_time(e1) / 1e3) / 1e6
+    # The float64 form is bound by the float64 pipe, not by HBM: per grid
+    # point and axis, 4 passes x ~12 float64 flops (add, add, fma, sub per
+    # cell of v and w, plus the chunk sums), 96 flops for two axes.  Peak:
+    # float64 matrix multiply of 4096^3 (cuBLAS), best of 3.
+    FP64_FLOPS_PER_GRIDPT = 96
+    a64 = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+    b64 = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+    torch.matmul(a64, b64)
+    dgemm = 0.0
+    for _ in range(3):
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        g0.record(stream)
+        torch.matmul(a64, b64)
+        g1.record(stream)
+        g1.synchronize()
+        dgemm = max(dgemm, 2 * 4096 ** 3 / (g0.elapsed_time(g1) * 1e-3) / 1e12)
+    del a64, b64
+    fp64_tflops = fp64_value * 1e6 * FP64_FLOPS_PER_GRIDPT / 1e12
     planq = BatchPlan(fields, precision=args.precision, out_dtype=np.float64, graph=False, knobs=knobs, device=dev)
     planq.run(stream)
     torch.cuda.synchronize()
@@ -498,7 +516,11 @@ def main():
                              "launch_ms": stage_ms[dom],
                              "stage_ms": {names[k]: v for k, v in stage_ms.items()},
                              "pipeline_gbs": pipeline_gbs, "pipeline_frac": pipeline_gbs / peak},
-                "fp64_form": {"value": fp64_value, "unit": "Mgridpts/s", "speedup_of_fp32c": value / fp64_value},
+                "fp64_form": {"value": fp64_value, "unit": "Mgridpts/s", "speedup_of_fp32c": value / fp64_value,
+                              "roofline": {"bound": "fp64", "flops_per_gridpt": FP64_FLOPS_PER_GRIDPT,
+                                           "achieved_tflops": fp64_tflops, "peak_tflops": dgemm,
+                                           "peak_kind": "measured float64 matmul 4096^3",
+                                           "frac": fp64_tflops / dgemm}},
                 "error_vs_fp64": {"rel_max": err_rel, "max_abs": err_abs, "rms": err_rms,
                                   "max_over_range": err_range, "mask_mismatch": mask_mismatch},
                 "error_vs_naive_subgrid": vs_naive,

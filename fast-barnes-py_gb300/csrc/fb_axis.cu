@@ -45,7 +45,7 @@ static int kchunk_of(int precision, int T, int kchunk)
 }
 
 static int cell_size(int precision) { return precision == 0 ? 16 : 8; }
-static int col_g(int precision) { return 32 / cell_size(precision); }
+static int col_g(int precision) { return (precision == 0 ? kColBytesF64 : kColBytesF32) / cell_size(precision); }
 int axis_col_group(int precision) { return col_g(precision); }
 constexpr int kMaxThreads = 512;
 

@@ -521,10 +521,13 @@ __device__ __forceinline__ void store_chunk_columns(const AxisLaunch &a, const T
     }
 }
 
-// Column-layout group width: 32 bytes of each grid row.
+// Column-layout group: G adjacent lines, B bytes of each grid row, V 16-byte
+// vectors a row.
 template <typename C>
 struct ColG {
-    static constexpr int G = 32 / (int)sizeof(C);
+    static constexpr int B = sizeof(C) == 8 ? kColBytesF32 : kColBytesF64;
+    static constexpr int G = B / (int)sizeof(C);
+    static constexpr int V = B / 16;
 };
 
 // SPLAT_DIM: 0 = the lines are loaded from src, 1..3 = they are filled by
@@ -702,21 +705,23 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
         const C *src = reinterpret_cast<const C *>(fp.src) + gbase;
         const int64_t es = a.elem_stride;
         {
-            // zero pad rows before and after the lines (two 16-byte vectors a row)
+            // zero pad rows before and after the lines (V 16-byte vectors a row)
+            constexpr int V = ColG<C>::V;
             uint4 *z = reinterpret_cast<uint4 *>(cells);
             const int back = P - HP - E;
-            for (int i = tid; i < 2 * (HP + back); i += nthr) {
-                const int r = i >> 1;
-                z[2 * (r < HP ? r : HP + E + (r - HP)) + (i & 1)] = make_uint4(0u, 0u, 0u, 0u);
+            for (int i = tid; i < V * (HP + back); i += nthr) {
+                const int r = i / V;
+                z[V * (r < HP ? r : HP + E + (r - HP)) + (i - r * V)] = make_uint4(0u, 0u, 0u, 0u);
             }
         }
         C *dcell = cells + (size_t)HP * G;
         if (vec_ok) {
-            // two 16-byte asynchronous copies per row of G cells
-            const int nv = 2 * E;
+            // V 16-byte asynchronous copies per row of G cells
+            constexpr int V = ColG<C>::V;
+            const int nv = V * E;
             uint4 *d_ = reinterpret_cast<uint4 *>(dcell);
             for (int i = tid; i < nv; i += nthr) {
-                const int row = i >> 1, h = i & 1;
+                const int row = i / V, h = i - row * V;
                 cp_async16(d_ + i, reinterpret_cast<const char *>(src + row * es) + 16 * h);
             }
             cp_async_wait_all();
@@ -930,10 +935,11 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
         } else {
             C *dst = reinterpret_cast<C *>(fp.dst) + gbase;
             if (vec_ok) {
-                const int nv = 2 * (s1 - s0);
+                constexpr int V = ColG<C>::V;
+                const int nv = V * (s1 - s0);
                 const uint4 *s_ = reinterpret_cast<const uint4 *>(dcell + (size_t)s0 * G);
                 for (int i = tid; i < nv; i += nthr) {
-                    const int row = s0 + (i >> 1), h = i & 1;
+                    const int row = s0 + i / V, h = i % V;
                     *reinterpret_cast<uint4 *>(reinterpret_cast<char *>(dst + row * es) + 16 * h) = s_[i];
                 }
             } else {
@@ -949,14 +955,16 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
 
 // Registers per thread (launches have at most 512 threads).  Float32
 // sliding passes with the short chunk fit in 64, so two 512-thread CTAs (or
-// four of 256) can share an SM; with the long chunk, rows fit in 96 without
-// spilling (five 128-thread CTAs an SM instead of four); the other variants
-// (columns with the long chunk, float64 cells, direct sums) keep 128.
+// four of 256) can share an SM; with the long chunk, rows (and columns in
+// 16-byte groups, 128-thread CTAs) fit in 96 without spilling (five CTAs an
+// SM instead of four); the other variants (columns in 32-byte groups with
+// the long chunk, float64 cells, direct sums) keep 128.
 template <typename Real, int K, int MODE, int LAYOUT>
 struct AxisRegs {
     static constexpr int value = (sizeof(Real) == 4 && MODE == 0 && K == K64)                  ? 64
-                                 : (sizeof(Real) == 4 && MODE == 0 && K == K32 && LAYOUT == 0) ? 96
-                                                                                               : 128;
+                                 : (sizeof(Real) == 4 && MODE == 0 && K == K32 && (LAYOUT == 0 || kColBytesF32 <= 16))
+                                     ? 96
+                                     : 128;
 };
 
 template <typename Real, int K, int MODE, int SPLAT_DIM, int LAYOUT>

@@ -145,6 +145,11 @@ struct BatchKeyField {
 };
 constexpr int kBatchKeysPerBlock = 512;
 
+// Bytes of each grid row that one columns-layout CTA holds (its G adjacent
+// lines interleaved): the float32 form's and the float64 form's.
+constexpr int kColBytesF32 = 32;
+constexpr int kColBytesF64 = 32;
+
 // Sorted-sample view handed to the splatting first-axis kernel.
 struct SampleView {
     const void *rec;              // SampleRec<Real> in sorted order (by bin, then sample)
