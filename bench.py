@@ -308,6 +308,12 @@ def main():
            1: B * (NPTS * 28 + W * H * 2 * sz),
            2: B * (W * H * 2 * sz + W * H * 4)}
     names = {0: "sample sort (6 kernels)", 1: "k_axis_batch x (splat fused)", 2: "k_axis_batch y (quotient fused)"}
+    # DRAM bytes (read + write) of each axis launch per field, from the ncu
+    # capture of the same kernels on 2 fields of this shape (the full-set
+    # capture of the profile summaries), scaled to B fields: the traffic
+    # grows with the fields processed (independent fields, each far larger
+    # than L2 once B >= 2)
+    traffic_per_field = {1: (6.505728e6 + 73.214208e6) / 2, 2: (134.617344e6 + 38.1568e6) / 2}
     stage_ms = {k: statistics.median(v) for k, v in per_stage.items()}
     dom = max((k for k in stage_ms if k != 0), key=lambda k: stage_ms[k])
     peak, peak_kind = measured_peak()
@@ -512,7 +518,10 @@ def main():
                 "gpu_launches": launches_per_step * args.steps,
                 "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
                              "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                             "traffic": None, "algorithmic_bytes_per_launch": alg[dom],
+                             "traffic": (traffic_per_field[dom] * B
+                                         if prec == _lib.FB_FP32C and (W, H) == (4096, 2048) else None),
+                             "traffic_source": "ncu capture of 2 fields, scaled to the batch",
+                             "algorithmic_bytes_per_launch": alg[dom],
                              "launch_ms": stage_ms[dom],
                              "stage_ms": {names[k]: v for k, v in stage_ms.items()},
                              "pipeline_gbs": pipeline_gbs, "pipeline_frac": pipeline_gbs / peak},
