@@ -61,6 +61,26 @@ def workload_config(batch, precision):
             "l2": "inputs larger than L2: each step touches ~%d MB of distinct field outputs" % (batch * W * H * 4 >> 20)}
 
 
+def uneven_batch_inputs(seed=512, count=512):
+    """The survey's batched configuration: `count` fields, grids (W, H) drawn
+    from 256x256, 1024x512, 2048x1024, N log-uniform in [500, 50000], sigma
+    uniform in [0.5, 4] grid steps, values a sum of 8 random-phase sinusoids
+    plus N(0, 1) noise, n = 4."""
+    rng = np.random.default_rng(seed)
+    grids = ((256, 256), (1024, 512), (2048, 1024))
+    out = []
+    step = 1.0 / 64
+    for _ in range(count):
+        gw, gh = grids[rng.integers(3)]
+        n = int(np.exp(rng.uniform(np.log(500), np.log(50000))))
+        sigma = float(rng.uniform(0.5, 4.0)) * step
+        pts = rng.uniform([0, 0], [gw * step, gh * step], (n, 2))
+        ph = rng.uniform(0, 2 * np.pi, 8)
+        val = sum(np.sin(pts[:, 0] * (q + 1) + ph[q]) for q in range(8)) + rng.normal(0, 1, n)
+        out.append((pts, val, sigma, step, (gw, gh)))
+    return out
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle samples while the timed region runs."""
 
@@ -498,6 +518,31 @@ def main():
     plan.close()
     plan2.close()
 
+    # ---- uneven batch: 512 fields of three grids, uneven N and sigma -------
+    ub = uneven_batch_inputs()
+    ub_fields = [dict(pts=torch.as_tensor(p_, device=dev), val=torch.as_tensor(v_, device=dev), sigma=sg, x0=(0.0, 0.0),
+                      step=stp, size=sz, num_iter=4) for p_, v_, sg, stp, sz in ub]
+    ub_plan = BatchPlan(ub_fields, precision=args.precision, graph=True, tune=True, device=dev)
+    for _ in range(3):
+        ub_plan.run(stream)
+    k_ub = max(3, args.steps // 4)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(k_ub):
+        ub_plan.run(stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ub_pts = sum(sz[0] * sz[1] for _, _, _, _, sz in ub)
+    ub_ms = e0.elapsed_time(e1) / k_ub
+    ub_launches, _, _ = ub_plan.info
+    uneven = {"value": ub_pts / (ub_ms / 1e3) / 1e6, "unit": "Mgridpts/s", "fields": len(ub),
+              "gridpts_per_run": ub_pts, "samples_per_run": int(sum(len(v_) for _, v_, _, _, _ in ub)),
+              "ms_per_run": ub_ms, "kernel_launches_per_run": ub_launches, "knobs": list(ub_plan.knobs),
+              "workload": "512 fields, grids 256x256 / 1024x512 / 2048x1024, N log-uniform 500..50000, "
+                          "sigma U[0.5, 4] steps, n = 4, one plan (CUDA graph)"}
+    ub_plan.close()
+    del ub_fields
+
     # ---- CPU baseline (rank 0, N = 1 only) ----------------------------------
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -533,6 +578,7 @@ def main():
                 "error_vs_fp64": {"rel_max": err_rel, "max_abs": err_abs, "rms": err_rms,
                                   "max_over_range": err_range, "mask_mismatch": mask_mismatch},
                 "error_vs_naive_subgrid": vs_naive,
+                "uneven_batch_form": uneven,
                 "single_call_form": {"value": single_value, "unit": "Mgridpts/s",
                                      "entry": "fb_interpolate once per field, inputs resident",
                                      "stage_ms_per_field": single_stage_ms},
