@@ -499,25 +499,27 @@ template <typename Real, typename C, int K>
 __device__ __forceinline__ void store_chunk_columns(const AxisLaunch &a, const TilePtrs &fp, int64_t gb, int a0,
                                                     int s0, int s1, Real thr, Real offs, const C (&o)[K])
 {
+    // (a path without the per-cell range checks for chunks wholly inside
+    // [s0, s1), chosen per warp, measured slower)
     const int64_t es = a.elem_stride;
     if (!a.store_quot) {
-        C *d_ = reinterpret_cast<C *>(fp.dst) + gb;
+        C *d_ = reinterpret_cast<C *>(fp.dst) + gb + (int64_t)a0 * es;
 #pragma unroll
         for (int i = 0; i < K; i++)
             if (a0 + i >= s0 && a0 + i < s1)
-                d_[(int64_t)(a0 + i) * es] = o[i];
+                d_[i * es] = o[i];
     } else if (a.out_f64) {
-        double *d_ = reinterpret_cast<double *>(fp.out) + gb;
+        double *d_ = reinterpret_cast<double *>(fp.out) + gb + (int64_t)a0 * es;
 #pragma unroll
         for (int i = 0; i < K; i++)
             if (a0 + i >= s0 && a0 + i < s1)
-                d_[(int64_t)(a0 + i) * es] = (double)quotient<Real>(o[i].x, o[i].y, thr, offs);
+                d_[i * es] = (double)quotient<Real>(o[i].x, o[i].y, thr, offs);
     } else {
-        float *d_ = reinterpret_cast<float *>(fp.out) + gb;
+        float *d_ = reinterpret_cast<float *>(fp.out) + gb + (int64_t)a0 * es;
 #pragma unroll
         for (int i = 0; i < K; i++)
             if (a0 + i >= s0 && a0 + i < s1)
-                d_[(int64_t)(a0 + i) * es] = (float)quotient<Real>(o[i].x, o[i].y, thr, offs);
+                d_[i * es] = (float)quotient<Real>(o[i].x, o[i].y, thr, offs);
     }
 }
 
@@ -759,9 +761,11 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
                     store_chunk_columns<Real, C, K>(a, fp, gbase + li, k0, s0, s1, thr, offs, o);
                 break;
             }
+            // per-cell checks only in warps holding the line's last chunk
+            const bool edge_warp = __any_sync(0xffffffffu, active && k0 + K > E);
             __syncthreads();
             if (active) {
-                if (k0 + K <= E) {
+                if (!edge_warp) {
 #pragma unroll
                     for (int i = 0; i < K; i++)
                         ln[(k0 + i) * ES] = o[i];
@@ -794,6 +798,10 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
             const bool left = (pass & 1) == 0;
             const bool more = pass + 1 < a.passes;
             const int a0 = left ? j * K - T - 1 : j * K;   // this pass's chunk
+            // Chunks reaching outside the line need per-cell clearing and
+            // stores; decided per warp (a uniform branch), so that warps
+            // without such a chunk skip the checks altogether.
+            const bool edge_warp = __any_sync(0xffffffffu, active && (a0 < 0 || a0 + K > E));
             C X = czero<C>();
             if (active) {
                 C mid = czero<C>();
@@ -820,7 +828,8 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
                     else
                         pass_right<C, K, ES, false>(ln, b, T, E, A0, A1, cu, o);
                 }
-                clip_chunk(o, a0, E);
+                if (edge_warp)
+                    clip_chunk(o, a0, E);
                 if (more) {
                     // the next pass goes the other way: it needs the first r
                     // cells of an A chunk, the last r of an F chunk
@@ -837,7 +846,7 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
             }
             __syncthreads();
             if (active) {
-                if (a0 >= 0 && a0 + K <= E) {
+                if (!edge_warp) {
 #pragma unroll
                     for (int i = 0; i < K; i++)
                         ln[(a0 + i) * ES] = o[i];
