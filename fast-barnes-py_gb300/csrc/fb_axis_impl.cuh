@@ -267,20 +267,29 @@ __device__ __forceinline__ void direct_dispatch(int T, const C *s, int k0, const
     }
 }
 
+// Pairwise sum of o[LO..HI) (zero for an empty range): a tree of depth
+// log2(HI - LO), so the sums do not wait on a chain of dependent adds.
+template <int LO, int HI, typename C, int K>
+__device__ __forceinline__ C tree_sum(const C (&o)[K])
+{
+    if constexpr (HI <= LO) {
+        return czero<C>();
+    } else if constexpr (HI - LO == 1) {
+        return o[LO];
+    } else {
+        constexpr int M = (LO + HI) / 2;
+        return cadd(tree_sum<LO, M>(o), tree_sum<M, HI>(o));
+    }
+}
+
 // The sums a chunk leaves for the next pass: S = o[0] + S1 with S1 the sum
 // of o[1..K-1], and X = the first R cells (PRE) or the last R cells (suffix),
-// each accumulated once over disjoint segments.
+// each accumulated once over disjoint segments (pairwise).
 template <typename C, int K, int R, bool PRE>
 __device__ __forceinline__ void chunk_sums_fixed(const C (&o)[K], C &S, C &S1, C &X)
 {
     constexpr int B = PRE ? (R > 0 ? R : 1) : (K - R > 1 ? K - R : 1);   // segment split inside [1, K)
-    C a = czero<C>(), z = czero<C>();
-#pragma unroll
-    for (int i = 1; i < B; i++)
-        a = cadd(a, o[i]);
-#pragma unroll
-    for (int i = B; i < K; i++)
-        z = cadd(z, o[i]);
+    const C a = tree_sum<1, B>(o), z = tree_sum<B, K>(o);
     S1 = cadd(a, z);
     S = cadd(o[0], S1);
     if (PRE)
