@@ -581,7 +581,8 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
         line0 = group * a.lines_per_cta;
         nl = (int)min((int64_t)a.lines_per_cta, a.nlines - line0);
     } else {
-        const int64_t o = group / a.xblocks, xb = group - o * a.xblocks;
+        const uint32_t o32 = (uint32_t)group / (uint32_t)a.xblocks;
+        const int64_t o = o32, xb = group - o * a.xblocks;
         nl = (int)min((int64_t)G, a.width - xb * G);
         gbase = o * a.outer_stride + xb * G + e0 * a.elem_stride;
         vec_ok = nl == G && (gbase % G) == 0 && (a.elem_stride % G) == 0;
@@ -593,7 +594,7 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
     const C *pp0;
     int QS;
     if (LAYOUT == 0) {
-        li = tid / CP;
+        li = NLC == 1 ? 0 : tid / CP;
         j = tid - li * CP;
         ln = cells + (size_t)li * P + HP;
         QS = NLC * PP;
@@ -985,34 +986,56 @@ struct AxisRegs {
                                      : 128;
 };
 
+// Block index -> (line group, tile along the lines); most launches have one
+// tile a line, and the indices fit 32 bits (a 64-bit division costs every
+// thread dozens of instructions).
+__device__ __forceinline__ void split_block(uint32_t b, int64_t ntiles, int64_t &group, int64_t &tile)
+{
+    if (ntiles == 1) {
+        group = b;
+        tile = 0;
+    } else {
+        const uint32_t gq = b / (uint32_t)ntiles;
+        group = gq;
+        tile = b - gq * (uint32_t)ntiles;
+    }
+}
+
 template <typename Real, int K, int MODE, int SPLAT_DIM, int LAYOUT>
 __global__ void __maxnreg__((AxisRegs<Real, K, MODE, LAYOUT>::value))
     k_axis(const AxisLaunch a, const Geometry g, const SampleView sv)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int64_t group = blockIdx.x / a.ntiles;
+    int64_t group, tile;
+    split_block(blockIdx.x, a.ntiles, group, tile);
     TilePtrs fp;
     fp.src = a.src_v;
     fp.dst = a.dst_v;
     fp.out = a.out;
     fp.bin_start = sv.bin_start;
     fp.hdr = sv.hdr;
-    axis_tile<Real, K, MODE, SPLAT_DIM, LAYOUT>(a, g, sv, fp, group, blockIdx.x - group * a.ntiles, smem_raw);
+    axis_tile<Real, K, MODE, SPLAT_DIM, LAYOUT>(a, g, sv, fp, group, tile, smem_raw);
 }
 
 // Batched form: fields of identical shape and parameters (one launch
-// description in kernel parameters, one TilePtrs per field); block x of the
-// grid is block x % bpf of field x / bpf.
+// description in kernel parameters, one TilePtrs per field); grid (bpf,
+// fields): block (x, y) is block x of field y (a one-dimensional grid of
+// bpf x fields blocks when there are more fields than grid rows).
 template <typename Real, int K, int MODE, int SPLAT_DIM, int LAYOUT>
 __global__ void __maxnreg__((AxisRegs<Real, K, MODE, LAYOUT>::value))
     k_axis_batch(const AxisLaunch a, const Geometry g, const SampleView sv, const TilePtrs *__restrict__ fields,
                  uint32_t blocks_per_field)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const uint32_t f = blockIdx.x / blocks_per_field, b = blockIdx.x - f * blocks_per_field;
+    uint32_t f = blockIdx.y, b = blockIdx.x;
+    if (gridDim.x != blocks_per_field) {
+        f = blockIdx.x / blocks_per_field;
+        b = blockIdx.x - f * blocks_per_field;
+    }
     const TilePtrs fp = fields[f];
-    const int64_t group = b / a.ntiles;
-    axis_tile<Real, K, MODE, SPLAT_DIM, LAYOUT>(a, g, sv, fp, group, b - group * a.ntiles, smem_raw);
+    int64_t group, tile;
+    split_block(b, a.ntiles, group, tile);
+    axis_tile<Real, K, MODE, SPLAT_DIM, LAYOUT>(a, g, sv, fp, group, tile, smem_raw);
 }
 
 // Mixed batched form: one launch for fields of different grids and
@@ -1034,9 +1057,9 @@ __global__ void __maxnreg__((AxisRegs<Real, K, MODE, LAYOUT>::value))
             dst[w] = src[w];
     }
     __syncthreads();
-    const int64_t group = it.y / s_f.a.ntiles;
-    axis_tile<Real, K, MODE, SPLAT_DIM, LAYOUT>(s_f.a, s_f.g, s_f.sv, s_f.fp, group, it.y - group * s_f.a.ntiles,
-                                                smem_raw);
+    int64_t group, tile;
+    split_block(it.y, s_f.a.ntiles, group, tile);
+    axis_tile<Real, K, MODE, SPLAT_DIM, LAYOUT>(s_f.a, s_f.g, s_f.sv, s_f.fp, group, tile, smem_raw);
 }
 
 // ---------------------------------------------------------------------------
@@ -1089,7 +1112,9 @@ static cudaError_t launch_batch_one(int op, const AxisLaunch &a, const Geometry 
     if (op == 1) {
         if (*grid < 1)
             return cudaSuccess;
-        k_axis_batch<Real, K, MODE, SD, LAY><<<(unsigned)*grid, threads, smem, st>>>(a, g, sv, fields, bpf);
+        const uint32_t nf = bpf > 0 ? nitems / bpf : 0;
+        const dim3 grid2 = nf <= 65535u && nf * bpf == nitems ? dim3(bpf, nf) : dim3((unsigned)*grid);
+        k_axis_batch<Real, K, MODE, SD, LAY><<<grid2, threads, smem, st>>>(a, g, sv, fields, bpf);
         return cudaGetLastError();
     }
     cudaError_t e = cudaFuncSetAttribute(k_axis_batch<Real, K, MODE, SD, LAY>,
