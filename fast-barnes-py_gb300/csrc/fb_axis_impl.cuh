@@ -508,27 +508,28 @@ template <typename Real, typename C, int K>
 __device__ __forceinline__ void store_chunk_columns(const AxisLaunch &a, const TilePtrs &fp, int64_t gb, int a0,
                                                     int s0, int s1, Real thr, Real offs, const C (&o)[K])
 {
-    // (a path without the per-cell range checks for chunks wholly inside
-    // [s0, s1), chosen per warp, measured slower)
+    // One pointer stepped by the row stride (no 64-bit multiply per cell).
+    // (A path without the range test for chunks wholly inside [s0, s1),
+    // chosen per warp, measured slower.)
     const int64_t es = a.elem_stride;
     if (!a.store_quot) {
         C *d_ = reinterpret_cast<C *>(fp.dst) + gb + (int64_t)a0 * es;
 #pragma unroll
-        for (int i = 0; i < K; i++)
+        for (int i = 0; i < K; i++, d_ += es)
             if (a0 + i >= s0 && a0 + i < s1)
-                d_[i * es] = o[i];
+                *d_ = o[i];
     } else if (a.out_f64) {
         double *d_ = reinterpret_cast<double *>(fp.out) + gb + (int64_t)a0 * es;
 #pragma unroll
-        for (int i = 0; i < K; i++)
+        for (int i = 0; i < K; i++, d_ += es)
             if (a0 + i >= s0 && a0 + i < s1)
-                d_[i * es] = (double)quotient<Real>(o[i].x, o[i].y, thr, offs);
+                *d_ = (double)quotient<Real>(o[i].x, o[i].y, thr, offs);
     } else {
         float *d_ = reinterpret_cast<float *>(fp.out) + gb + (int64_t)a0 * es;
 #pragma unroll
-        for (int i = 0; i < K; i++)
+        for (int i = 0; i < K; i++, d_ += es)
             if (a0 + i >= s0 && a0 + i < s1)
-                d_[i * es] = (float)quotient<Real>(o[i].x, o[i].y, thr, offs);
+                *d_ = (float)quotient<Real>(o[i].x, o[i].y, thr, offs);
     }
 }
 
