@@ -5,10 +5,11 @@
 // (fastbarnes/interpolation.py:218-322: cell index, skip rule) and
 // _normalize_values (:204-212: min/max of the values).
 //
-// Samples are counted per bin (grid row, or (z, y) row, or x range in 1D),
-// the counts are scanned into bin starts, every sample is placed into its bin
-// with an atomic cursor, and finally every bin is sorted by sample index, so
-// the order inside a bin is the samples' own order whatever the atomics did.
+// Samples are counted per bin (grid row, or (z, y) row, or x range in 1D) by
+// atomics whose returned counts give every sample a slot in its bin, the
+// counts are scanned into bin starts, every sample is placed into its slot,
+// and finally every bin is sorted by sample index, so the order inside a bin
+// is the samples' own order whatever the atomics did.
 // The splatting kernel then adds each row's samples in that order.
 #include <algorithm>
 
@@ -61,7 +62,8 @@ __device__ __forceinline__ void range_to_header(unsigned long long kmin, unsigne
 template <int DIM, typename Real>
 __global__ void k_bin_keys(const double *__restrict__ pts, const double *__restrict__ val, int64_t npts,
                            Geometry g, int bin_w, uint32_t nbins, uint32_t *__restrict__ keys,
-                           SampleRec<Real> *__restrict__ rec, uint32_t *__restrict__ counts, FieldHeader *hdr)
+                           SampleRec<Real> *__restrict__ rec, uint32_t *__restrict__ counts,
+                           uint32_t *__restrict__ rank, FieldHeader *hdr)
 {
     // float64 instructions kept to the cell coordinates, as in k_batch_keys
     constexpr bool EXACT = sizeof(Real) == 8;
@@ -123,7 +125,7 @@ __global__ void k_bin_keys(const double *__restrict__ pts, const double *__restr
         rec[k] = r;
         keys[k] = key;
         if (key < nbins)
-            atomicAdd(&counts[key], 1u);
+            rank[k] = atomicAdd(&counts[key], 1u);   // the sample's slot in its bin (any order)
     }
     range_to_header(kmin, kmax, nan, hdr);
 }
@@ -184,16 +186,17 @@ __global__ void __launch_bounds__(1024) k_scan_exclusive(const uint32_t *__restr
     }
 }
 
-// Places every sample into its bin; the order inside a bin is fixed later.
+// Places every sample into the slot of its bin that the key kernel drew; the
+// order inside a bin is fixed later.
 __global__ void k_bin_scatter(const uint32_t *__restrict__ keys, int64_t npts, uint32_t nbins,
-                              const uint32_t *__restrict__ start, uint32_t *__restrict__ cursor,
+                              const uint32_t *__restrict__ start, const uint32_t *__restrict__ rank,
                               uint32_t *__restrict__ sorted)
 {
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < npts;
          k += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t key = keys[k];
         if (key < nbins)
-            sorted[start[key] + atomicAdd(&cursor[key], 1u)] = (uint32_t)k;
+            sorted[start[key] + rank[k]] = (uint32_t)k;
     }
 }
 
@@ -330,7 +333,8 @@ __global__ void __launch_bounds__(1024) k_sort_large(const uint32_t *__restrict_
 template <typename Real>
 __global__ void k_batch_keys(const BatchKeyField *__restrict__ fields, const uint2 *__restrict__ blocks,
                              uint32_t skip_key, uint32_t *__restrict__ keys, SampleRec<Real> *__restrict__ rec,
-                             uint32_t *__restrict__ counts, FieldHeader *__restrict__ hdrs)
+                             uint32_t *__restrict__ counts, uint32_t *__restrict__ rank,
+                             FieldHeader *__restrict__ hdrs)
 {
     // Float64 instructions are few per SM on this part, so the loop keeps
     // them to the cell coordinates: the NaN test works on the bits, the
@@ -389,7 +393,7 @@ __global__ void k_batch_keys(const BatchKeyField *__restrict__ fields, const uin
         rec[gk] = r;
         keys[gk] = key;
         if (key < skip_key)
-            atomicAdd(&counts[key], 1u);
+            rank[gk] = atomicAdd(&counts[key], 1u);   // the sample's slot in its bin (any order)
     }
     range_to_header(kmin, kmax, nan, hdrs + bt.x);
 }
@@ -469,7 +473,8 @@ __global__ void __launch_bounds__(1024) k_tile_scan(const uint32_t *__restrict__
 
 
 // Scratch layout: counts[nbins + 2] | cursor[nbins + 2] | large[nbins + 2] |
-// keys[N] | sorted[N] | big-bin scratch[2N] (uint32), then the sample records
+// keys[N] | sorted[N] | big-bin scratch[2N] (uint32; its first N entries hold
+// the samples' slots in their bins until the scatter), then the sample records
 // by sample index, the records in sorted order, and (batched form) the
 // per-tile sums of the device-wide scan.
 namespace {
@@ -562,11 +567,11 @@ cudaError_t batch_sort(int precision, const BatchKeyField *d_fields, const uint2
         if (precision == 0)
             k_batch_keys<double><<<nblocks, 256, 0, st>>>(d_fields, d_blocks, nbins, l.keys,
                                                            reinterpret_cast<SampleRec<double> *>(l.rec), l.counts,
-                                                           hdrs);
+                                                           l.big, hdrs);
         else
             k_batch_keys<float><<<nblocks, 256, 0, st>>>(d_fields, d_blocks, nbins, l.keys,
                                                           reinterpret_cast<SampleRec<float> *>(l.rec), l.counts,
-                                                          hdrs);
+                                                          l.big, hdrs);
     }
     const int64_t n = (int64_t)nbins + 1;
     const unsigned tiles = (unsigned)((n + 4095) / 4096);
@@ -576,7 +581,7 @@ cudaError_t batch_sort(int precision, const BatchKeyField *d_fields, const uint2
     k_tile_scan<<<tiles, 1024, 0, st>>>(l.counts, n, toff, bin_start);
     if (ntot > 0) {
         int blocks = (int)std::min<int64_t>((ntot + 255) / 256, (int64_t)1 << 22);
-        k_bin_scatter<<<blocks, 256, 0, st>>>(l.keys, ntot, nbins, bin_start, l.cursor, l.sorted);
+        k_bin_scatter<<<blocks, 256, 0, st>>>(l.keys, ntot, nbins, bin_start, l.big, l.sorted);
         const int rw = (int)(rec_bytes(precision) / 16);
         const uint4 *rec4 = reinterpret_cast<const uint4 *>(l.rec);
         uint4 *srec4 = reinterpret_cast<uint4 *>(l.srec);
@@ -603,7 +608,7 @@ cudaError_t sort_samples(int precision, const double *pts, const double *val, in
         int blocks = (int)std::min<int64_t>((npts + 255) / 256, (int64_t)1 << 22);
 #define FBG_KEYS(D, R)                                                                                            \
     k_bin_keys<D, R><<<blocks, 256, 0, st>>>(pts, val, npts, g, bin_w, nbins, l.keys,                              \
-                                             reinterpret_cast<SampleRec<R> *>(l.rec), l.counts, hdr)
+                                             reinterpret_cast<SampleRec<R> *>(l.rec), l.counts, l.big, hdr)
         if (precision == 0) {
             if (g.dim == 1)
                 FBG_KEYS(1, double);
@@ -624,7 +629,7 @@ cudaError_t sort_samples(int precision, const double *pts, const double *val, in
     k_scan_exclusive<<<1, 1024, 0, st>>>(l.counts, bin_start, (int64_t)nbins + 1);
     if (npts > 0) {
         int blocks = (int)std::min<int64_t>((npts + 255) / 256, (int64_t)1 << 22);
-        k_bin_scatter<<<blocks, 256, 0, st>>>(l.keys, npts, nbins, bin_start, l.cursor, l.sorted);
+        k_bin_scatter<<<blocks, 256, 0, st>>>(l.keys, npts, nbins, bin_start, l.big, l.sorted);
         const int rw = (int)(rec_bytes(precision) / 16);
         const uint4 *rec4 = reinterpret_cast<const uint4 *>(l.rec);
         uint4 *srec4 = reinterpret_cast<uint4 *>(l.srec);
