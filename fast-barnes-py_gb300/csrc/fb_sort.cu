@@ -242,7 +242,7 @@ __device__ __forceinline__ void copy_rec(const uint4 *__restrict__ rec, uint4 *_
 }
 
 // Sorts every bin's entries by sample index: one warp per bin, in registers for
-// up to 32 entries, in shared memory up to kWarpSortMax; larger bins are listed
+// up to 64 entries, in shared memory up to kWarpSortMax; larger bins are listed
 // for k_sort_large.  Every sorted bin also gets its sample records copied into
 // sorted order (rw 16-byte words a record).
 __global__ void __launch_bounds__(32 * kBinSortWarps) k_sort_bins(const uint32_t *__restrict__ start, uint32_t nbins,
@@ -275,8 +275,40 @@ __global__ void __launch_bounds__(32 * kBinSortWarps) k_sort_bins(const uint32_t
         }
         return;
     }
+    if (c <= 64) {
+        // two keys a lane (elements lane and lane + 32), bitonic network in
+        // registers: partners 32 apart sit in the same lane, the others are
+        // a shuffle away
+        uint32_t x0 = lane < (int)c ? sorted[s0 + lane] : 0xFFFFFFFFu;
+        uint32_t x1 = lane + 32 < (int)c ? sorted[s0 + lane + 32] : 0xFFFFFFFFu;
+        for (int k = 2; k <= 64; k <<= 1) {
+            for (int jj = k >> 1; jj > 0; jj >>= 1) {
+                if (jj == 32) {   // k = 64: ascending everywhere
+                    const uint32_t lo = min(x0, x1), hi = max(x0, x1);
+                    x0 = lo;
+                    x1 = hi;
+                } else {
+                    const uint32_t y0 = __shfl_xor_sync(0xffffffffu, x0, jj);
+                    const uint32_t y1 = __shfl_xor_sync(0xffffffffu, x1, jj);
+                    const bool lower = (lane & jj) == 0;
+                    const bool asc0 = (lane & k) == 0, asc1 = ((lane + 32) & k) == 0;
+                    x0 = (lower == asc0) ? min(x0, y0) : max(x0, y0);
+                    x1 = (lower == asc1) ? min(x1, y1) : max(x1, y1);
+                }
+            }
+        }
+        if (lane < (int)c) {
+            sorted[s0 + lane] = x0;
+            copy_rec(rec, srec, rw, x0, s0 + lane);
+        }
+        if (lane + 32 < (int)c) {
+            sorted[s0 + lane + 32] = x1;
+            copy_rec(rec, srec, rw, x1, s0 + lane + 32);
+        }
+        return;
+    }
     if (c <= kWarpSortMax) {
-        int n = 64;
+        int n = 128;
         while (n < (int)c)
             n <<= 1;
         uint32_t *s = buf[w];
