@@ -2,8 +2,8 @@
 
 TEST INFRASTRUCTURE, NOT PRODUCT CODE: only tests/, the smoke check in
 __graft_entry__.py and bench.py's CPU-baseline / reference arm use this module,
-and only as the checker or the timed CPU baseline.  The GPU library never
-imports it.
+and only to compare the GPU results against or as the timed CPU baseline.
+The GPU library never imports it.
 
 Every function mirrors one of the reference's (MeteoSwiss/fast-barnes-py) in
 its float64 operation order; see the citations in barnes_oracle.c.
