@@ -25,9 +25,10 @@
 // from per-chunk partial sums of the previous pass that lie entirely inside
 // the window, so nothing cancels), slides forward over the first half of the
 // chunk and backward over the second half, keeps the K outputs in registers,
-// and writes them back in place after a barrier.  K is odd, so the lanes of a
-// warp (consecutive chunks) spread over all banks.  Narrow kernels sum every
-// output directly from registers instead.
+// and writes them back in place after a barrier (the last pass of a columns
+// launch stores them to HBM from registers instead).  K is odd, so the lanes
+// of a warp (consecutive chunks) spread over all banks.  Narrow kernels sum
+// every output directly from registers instead.
 //
 // Window semantics are the reference's (interpolation.py:500-523): out[k] =
 // sum_{|d|<=T} in[k+d] + alpha * (in[k-T-1] + in[k+T+1]), in[] = 0 outside
