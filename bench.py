@@ -327,7 +327,7 @@ def main():
     alg = {0: B * NPTS * (24 + 4 * 6),
            1: B * (NPTS * 28 + W * H * 2 * sz),
            2: B * (W * H * 2 * sz + W * H * 4)}
-    names = {0: "sample sort (6 kernels)", 1: "k_axis_batch x (splat fused)", 2: "k_axis_batch y (quotient fused)"}
+    names = {0: "sample sort", 1: "k_axis_batch x (splat fused)", 2: "k_axis_batch y (quotient fused)"}
     # DRAM bytes (read + write) of each axis launch per field, from the ncu
     # capture of the same kernels on 2 fields of this shape (the full-set
     # capture of the profile summaries), scaled to B fields: the traffic

@@ -1602,11 +1602,13 @@ extern "C" int fb_batch_info(const fb_batch *b, int *kernel_launches, int *memse
 {
     if (!b)
         return fail(FB_ERR_ARG, "null plan");
-    // batch_sort: k_batch_keys (when there are samples), k_tile_sums,
-    // k_scan_exclusive, k_tile_scan, then k_bin_scatter, k_sort_bins and
-    // k_sort_large (which also put the records in sorted order) when there
-    // are samples, and two memsets; then one axis launch per stage with work
-    int k = 3 + (b->nblocks > 0 ? 1 : 0) + (b->ntot > 0 ? 3 : 0);
+    // batch_sort: k_batch_keys (when there are samples), the bin-start scan
+    // (one launch, or k_tile_sums, k_scan_exclusive and k_tile_scan for many
+    // bins), then k_bin_scatter, k_sort_bins and k_sort_large (which also put
+    // the records in sorted order) when there are samples, and two memsets;
+    // then one axis launch per stage with work
+    const int scans = (int64_t)b->nbins + 1 <= kOneBlockScanMax ? 1 : 3;
+    int k = scans + (b->nblocks > 0 ? 1 : 0) + (b->ntot > 0 ? 3 : 0);
     for (const BatchStage &s : b->stages)
         k += s.grid > 0 ? 1 : 0;
     if (kernel_launches)

@@ -606,11 +606,15 @@ cudaError_t batch_sort(int precision, const BatchKeyField *d_fields, const uint2
                                                           l.big, hdrs);
     }
     const int64_t n = (int64_t)nbins + 1;
-    const unsigned tiles = (unsigned)((n + 4095) / 4096);
-    k_tile_sums<<<tiles, 1024, 0, st>>>(l.counts, n, l.tsum);
-    uint32_t *toff = l.tsum + tiles;
-    k_scan_exclusive<<<1, 1024, 0, st>>>(l.tsum, toff, (int64_t)tiles);
-    k_tile_scan<<<tiles, 1024, 0, st>>>(l.counts, n, toff, bin_start);
+    if (n <= kOneBlockScanMax) {
+        k_scan_exclusive<<<1, 1024, 0, st>>>(l.counts, bin_start, n);
+    } else {
+        const unsigned tiles = (unsigned)((n + 4095) / 4096);
+        k_tile_sums<<<tiles, 1024, 0, st>>>(l.counts, n, l.tsum);
+        uint32_t *toff = l.tsum + tiles;
+        k_scan_exclusive<<<1, 1024, 0, st>>>(l.tsum, toff, (int64_t)tiles);
+        k_tile_scan<<<tiles, 1024, 0, st>>>(l.counts, n, toff, bin_start);
+    }
     if (ntot > 0) {
         int blocks = (int)std::min<int64_t>((ntot + 255) / 256, (int64_t)1 << 22);
         k_bin_scatter<<<blocks, 256, 0, st>>>(l.keys, ntot, nbins, bin_start, l.big, l.sorted);
