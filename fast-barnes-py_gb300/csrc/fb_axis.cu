@@ -70,7 +70,9 @@ static int even(int64_t x) { return (int)((x + 1) / 2 * 2); }
 // (their chunks alternate between two grids T + 1 cells apart; a chunk that
 // lies wholly outside [0, E) in a pass reads clamped cells and is cleared).
 // Every read lies in [-(T + 1 + K), E + T + K): the line buffer has
-// T + 1 + K zero cells before the line and T + K after it.  The two partial-sum arrays (S, X) have q + 1
+// T + 1 + K zero cells before the line (one more when that is odd, so that
+// cell 0 of a float32 line is 16-byte aligned for vector stores) and T + K
+// after it.  The two partial-sum arrays (S, X) have q + 1
 // zero slots on both sides, q = floor((2T + 1)/K).
 static void set_geometry(int precision, AxisLaunch &a, int K, int64_t E)
 {
@@ -79,7 +81,7 @@ static void set_geometry(int precision, AxisLaunch &a, int K, int64_t E)
     const int unit = a.layout == 0 ? 32 : 32 / col_g(precision);
     a.chunks_pad = (nact + unit - 1) / unit * unit;
     a.extent_max = (int)E;
-    a.line_pad = a.T + 1 + K;
+    a.line_pad = (a.T + 1 + K + 1) & ~1;
     a.line_pitch = even((int64_t)a.line_pad + E + a.T + K);
     const int q = (2 * a.T + 1) / K;
     a.part_pad = q + 1;

@@ -118,6 +118,21 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
+// Bulk copy of `bytes` (a multiple of 16) from shared to global memory, both
+// addresses 16-byte aligned, by the tensor memory accelerator; the shared
+// data was written by the CTA's threads before a barrier, so the issuing
+// thread first orders those writes before the copy's reads (proxy fence).
+__device__ __forceinline__ void bulk_store(void *gmem, const void *smem, unsigned bytes)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;\n" ::"l"(gmem), "r"(s), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
+}
+// Waits until the issuing thread's bulk copies have read their shared source.
+__device__ __forceinline__ void bulk_store_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory"); }
+
 // ---------------------------------------------------------------------------
 // one line seen by one thread: cell e lives at s[e * ES]; the line buffer has
 // zero cells on both sides (T + 1 before the line, up to the end of the last
@@ -904,7 +919,15 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
                     d_[e] = c_[e].x;
             } else {
                 C *d_ = reinterpret_cast<C *>(fp.dst) + gb;
-                if (sizeof(C) == 8 && ((gb + s0) & 1) == 0 && ((HP + s0) & 1) == 0) {
+                if (sizeof(C) == 16 ||
+                    (((gb + s0) & 1) == 0 && ((HP + s0) & 1) == 0 && ((s1 - s0) & 1) == 0)) {
+                    // the line's cells as one bulk copy shared -> global
+                    // (tensor memory accelerator), issued by one thread after
+                    // the barrier above: both ends 16-byte aligned, a
+                    // multiple of 16 bytes
+                    if (tid == 0)
+                        bulk_store(d_ + s0, c_ + s0, (unsigned)((s1 - s0) * sizeof(C)));
+                } else if (sizeof(C) == 8 && ((gb + s0) & 1) == 0 && ((HP + s0) & 1) == 0) {
                     // pairs of float2 cells as 16-byte vectors
                     const int np = (s1 - s0) / 2;
                     const uint4 *sv4 = reinterpret_cast<const uint4 *>(c_ + s0);
@@ -919,6 +942,9 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
                 }
             }
         }
+        // the line buffer must outlive the bulk copies' reads of it
+        if (tid == 0)
+            bulk_store_wait_read();
     } else {
         const int64_t es = a.elem_stride;
         const C *dcell = cells + (size_t)HP * G;
