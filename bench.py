@@ -333,7 +333,7 @@ def main():
     # capture of the profile summaries), scaled to B fields: the traffic
     # grows with the fields processed (independent fields, each far larger
     # than L2 once B >= 2)
-    traffic_per_field = {1: (6.511616e6 + 73.408768e6) / 2, 2: (135.1488e6 + 38.130176e6) / 2}
+    traffic_per_field = {1: (6.503168e6 + 72.670208e6) / 2, 2: (135.293696e6 + 38.670848e6) / 2}
     stage_ms = {k: statistics.median(v) for k, v in per_stage.items()}
     dom = max((k for k in stage_ms if k != 0), key=lambda k: stage_ms[k])
     peak, peak_kind = measured_peak()
