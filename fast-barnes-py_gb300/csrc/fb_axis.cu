@@ -146,8 +146,10 @@ bool axis_shape(int precision, AxisLaunch &a)
         a.lines_per_cta = col_g(precision);
         return axis_threads(precision, a) <= kMaxThreads && axis_smem_bytes(precision, a) <= axis_smem_limit();
     }
-    // rows: ~256 threads per CTA unless the plan asks for another target
-    const int target = a.rows_threads > 0 ? a.rows_threads : 256;
+    // rows: ~128 threads per CTA (the batch autotuner's usual choice: five
+    // CTAs an SM, one line each for lines of ~4k cells) unless the plan asks
+    // for another target
+    const int target = a.rows_threads > 0 ? a.rows_threads : 128;
     int nl = std::max(1, std::min<int>(std::max(1, target / a.chunks_pad), kMaxThreads / a.chunks_pad));
     if (nl > a.nlines)
         nl = (int)a.nlines;

@@ -180,7 +180,7 @@ typedef struct fb_field2d {
 
 typedef struct fb_batch_knobs {
     int chunk;                /* 0 automatic, 17 or 33 (float32 windows wider than 65) */
-    int rows_threads;         /* x-axis threads per CTA target: 0 (= 256), 128, 256 or 512 */
+    int rows_threads;         /* x-axis threads per CTA target: 0 (= 128), 128, 256 or 512 */
     int mixed;                /* 1: per-field descriptions even when the fields share one shape */
 } fb_batch_knobs;
 
