@@ -62,7 +62,7 @@ def workload_config(batch, precision):
 
 
 def uneven_batch_inputs(seed=512, count=512):
-    """The survey's batched configuration: `count` fields, grids (W, H) drawn
+    """The uneven batched workload: `count` fields, grids (W, H) drawn
     from 256x256, 1024x512, 2048x1024, N log-uniform in [500, 50000], sigma
     uniform in [0.5, 4] grid steps, values a sum of 8 random-phase sinusoids
     plus N(0, 1) noise, n = 4."""
