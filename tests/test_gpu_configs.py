@@ -63,6 +63,36 @@ def test_sweep_fp32c_within_tolerance(W, H):
     assert worst > 0.0
 
 
+def test_sweep_full_factorial_fp32c_4096x2048():
+    """All 54 combinations of N {10k, 100k, 1M} x {uniform, 3-cluster} x
+    sigma {0.5, 1, 4} degrees x n {3, 4, 6} on the 4096 x 2048 grid: the
+    FP32C form within 1e-5 relative max error of the FP64 form, masks equal
+    but for at most 1e-6 of the points."""
+    import torch
+    W, H = 4096, 2048
+    rng = np.random.default_rng(2048)
+    x0, step = (-26.0, 34.5), (75.0 / W, 37.5 / H)
+    worst = 0.0
+    for N in (10_000, 100_000, 1_000_000):
+        for kind in ("uniform", "cluster"):
+            pts = locations(rng, N, kind)
+            val = 1000 + 20 * np.sin(pts[:, 0] / 10) * np.cos(pts[:, 1] / 8) + rng.normal(0, 2, N)
+            tp = torch.as_tensor(pts, device="cuda")
+            tv = torch.as_tensor(val, device="cuda")
+            for sigma in (0.5, 1.0, 4.0):
+                for n in (3, 4, 6):
+                    q64 = I.barnes(tp, tv, sigma, x0, step, (W, H), num_iter=n, out_dtype=np.float64)
+                    q32 = I.barnes(tp, tv, sigma, x0, step, (W, H), num_iter=n, out_dtype=np.float64,
+                                   precision="fp32c")
+                    nan64, nan32 = torch.isnan(q64), torch.isnan(q32)
+                    assert int((nan64 != nan32).sum()) <= 1e-6 * W * H, (N, kind, sigma, n)
+                    both = ~nan64 & ~nan32
+                    e = float((q32[both] - q64[both]).abs().max() / q64[both].abs().max())
+                    worst = max(worst, e)
+                    assert e <= 1e-5, (N, kind, sigma, n, e)
+    assert worst > 0.0
+
+
 def test_batch_of_512_uneven_fields():
     import torch
     rng = np.random.default_rng(512)

@@ -206,6 +206,39 @@ def test_clustered_sweep_vs_oracle():
         check_fp32c(q32, ref_q, wg, thr)
 
 
+def test_sweep_full_factorial_vs_oracle():
+    """Every combination of the 2D precision sweep's parameters on its
+    1024 x 512 grid (European domain, step 75/1024 x 37.5/512 degrees): N in
+    {10k, 100k, 1M}, uniform or 3-cluster locations, sigma in {0.5, 1, 4}
+    degrees, n in {3, 4, 6} -- 54 fields.  The float64 form within 1e-9 of
+    the oracle (its float32 result within 1 ulp), the float32-compensated
+    form within 1e-5 relative (both modes: sigma = 4, n = 6 at N = 1M grows
+    past the float32 limit, so its passes run scaled)."""
+    rng = np.random.default_rng(54)
+    x0, size = np.array([-26.0, 34.5]), (1024, 512)
+    step = np.array([75.0 / 1024, 37.5 / 512])
+    worst64 = worst32 = 0.0
+    for N in (10_000, 100_000, 1_000_000):
+        for kind in ("uniform", "cluster"):
+            if kind == "uniform":
+                pts = np.c_[rng.uniform(-26, 49, N), rng.uniform(34.5, 72, N)]
+            else:
+                c = rng.uniform([-20, 40], [40, 65], (3, 2))
+                s = rng.uniform(3, 8, 3)
+                lab = rng.integers(0, 3, N)
+                pts = c[lab] + rng.normal(0, 1, (N, 2)) * s[lab][:, None]
+            val = 1000 + 20 * np.sin(pts[:, 0] / 10) * np.cos(pts[:, 1] / 8) + rng.normal(0, 2, N)
+            for sigma in (0.5, 1.0, 4.0):
+                for n in (3, 4, 6):
+                    ref_out, ref_q, wg, thr = oracle.interpolate(pts, val, sigma, x0, step, size, n, nthreads=8)
+                    q = gpu(pts, val, sigma, x0, step, size, n, out_dtype=np.float64)
+                    out32 = gpu(pts, val, sigma, x0, step, size, n)
+                    worst64 = max(worst64, check_fp64(q, out32, ref_q, ref_out, wg, thr, val))
+                    q32 = gpu(pts, val, sigma, x0, step, size, n, precision="fp32c", out_dtype=np.float64)
+                    worst32 = max(worst32, check_fp32c(q32, ref_q, wg, thr))
+    assert worst32 > 0.0
+
+
 def test_3d_vs_oracle():
     rng = np.random.default_rng(21)
     N = 5000
