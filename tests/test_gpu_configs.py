@@ -11,8 +11,9 @@ seconds.
 - 1D L = 2^26, N = 4M: FP64 against the oracle on sub-lines (1e-9 relative
   to the value range) and on the whole line (1e-7: the reference's single
   running sum drifts over 2^26 cells), FP32C against FP64 (1e-5).
-- 3D 512 x 512 x 256, N = 2M: FP32C against FP64 (1e-5); a constant field
-  stays constant wherever it is not masked (exact property of V / W).
+- 3D 512 x 512 x 256, N = 2M: FP64 against the oracle on the whole volume
+  (1e-9), FP32C against FP64 (1e-5); a constant field stays constant wherever
+  it is not masked (exact property of V / W).
 """
 import numpy as np
 import pytest
@@ -180,6 +181,25 @@ def test_3d_full_size_and_constant_field():
     q32 = I.barnes(tp, tv, sigma, (0, 0, 0), step, size, num_iter=4, out_dtype=np.float64, precision="fp32c")
     a, b = q32.cpu().numpy(), q64.cpu().numpy()
     assert rel_err(a, b) <= 1e-5
+    # FP64 against the oracle on the whole volume: the float64 quotient within
+    # 1e-9 of max(|ref|, range(val)); the float32 result within 1 ulp plus
+    # that float64 tolerance (the values cross zero, where a float32 ulp is
+    # far below it, and rounding two float64 values to float32 keeps them
+    # within their distance plus an ulp); masks equal but where the weight is
+    # within 1e-9 of the mask level
+    ref_out, ref_q, wg, thr = oracle.interpolate(pts, val, np.array(sigma), np.zeros(3), np.array(step), size, 4,
+                                                 nthreads=16)
+    out32 = I.barnes(tp, tv, sigma, (0, 0, 0), step, size, num_iter=4).cpu().numpy()
+    diff = np.isnan(b) != np.isnan(ref_q)
+    assert np.all(np.abs(wg[diff] - thr) <= 1e-9 * abs(thr))
+    m = ~np.isnan(b) & ~np.isnan(ref_q)
+    assert m.any()
+    scale = np.maximum(np.abs(ref_q[m]), np.ptp(val))
+    assert np.max(np.abs(b[m] - ref_q[m]) / scale) <= 1e-9
+    m32 = ~np.isnan(out32) & ~np.isnan(ref_out)
+    tol32 = np.spacing(np.abs(ref_out[m32])).astype(np.float64) + 1e-9 * np.maximum(np.abs(ref_q[m32]), np.ptp(val))
+    assert np.all(np.abs(out32[m32].astype(np.float64) - ref_out[m32]) <= tol32)
+    del ref_out, ref_q, wg, out32
     const = torch.full_like(tv, 7.25)
     for prec in ("fp64", "fp32c"):
         f = I.barnes(tp, const, sigma, (0, 0, 0), step, size, num_iter=4, out_dtype=np.float64,
