@@ -30,6 +30,23 @@ def rel_err(a, b):
     return float(np.max(np.abs(a[m] - b[m])) / np.max(np.abs(b[m])))
 
 
+def check_fp64_vs_oracle(q64, out32, ref_out, ref_q, wg, thr, val):
+    """The float64 quotient within 1e-9 of max(|ref|, range(val)); the float32
+    result within 1 ulp plus that float64 tolerance (where values cross zero a
+    float32 ulp is far below it, and rounding two float64 values to float32
+    keeps them within their distance plus an ulp); NaN masks equal but where
+    the weight is within 1e-9 of the mask level."""
+    diff = np.isnan(q64) != np.isnan(ref_q)
+    assert np.all(np.abs(wg[diff] - thr) <= 1e-9 * abs(thr))
+    m = ~np.isnan(q64) & ~np.isnan(ref_q)
+    assert m.any()
+    scale = np.maximum(np.abs(ref_q[m]), np.ptp(val))
+    assert np.max(np.abs(q64[m] - ref_q[m]) / scale) <= 1e-9
+    m32 = ~np.isnan(out32) & ~np.isnan(ref_out)
+    tol32 = np.spacing(np.abs(ref_out[m32])).astype(np.float64) + 1e-9 * np.maximum(np.abs(ref_q[m32]), np.ptp(val))
+    assert np.all(np.abs(out32[m32].astype(np.float64) - ref_out[m32]) <= tol32)
+
+
 def locations(rng, N, kind):
     if kind == "uniform":
         return np.c_[rng.uniform(-26, 49, N), rng.uniform(34.5, 72, N)]
@@ -92,6 +109,31 @@ def test_sweep_full_factorial_fp32c_4096x2048():
                     worst = max(worst, e)
                     assert e <= 1e-5, (N, kind, sigma, n, e)
     assert worst > 0.0
+
+
+@pytest.mark.parametrize("W,H,N", [(4096, 2048, 100_000), (16384, 8192, 1_000_000)])
+def test_full_grids_vs_oracle(W, H, N):
+    """The headline field (4096 x 2048, N = 100k) and the sweep's largest grid
+    (16384 x 8192, N = 1M), uniform samples, sigma = 1 degree, n = 4: FP64
+    against the oracle over the whole grid, FP32C within 1e-5 relative of the
+    oracle (masks equal but within 1e-4 of the mask level)."""
+    import torch
+    rng = np.random.default_rng(W + N)
+    x0, step, sigma, n = (-26.0, 34.5), (75.0 / W, 37.5 / H), 1.0, 4
+    pts = locations(rng, N, "uniform")
+    val = 1000 + 20 * np.sin(pts[:, 0] / 10) * np.cos(pts[:, 1] / 8) + rng.normal(0, 2, N)
+    tp, tv = torch.as_tensor(pts, device="cuda"), torch.as_tensor(val, device="cuda")
+    ref_out, ref_q, wg, thr = oracle.interpolate(pts, val, sigma, np.array(x0), np.array(step), (W, H), n,
+                                                 nthreads=16)
+    q64 = I.barnes(tp, tv, sigma, x0, step, (W, H), num_iter=n, out_dtype=np.float64).cpu().numpy()
+    out32 = I.barnes(tp, tv, sigma, x0, step, (W, H), num_iter=n).cpu().numpy()
+    check_fp64_vs_oracle(q64, out32, ref_out, ref_q, wg, thr, val)
+    del q64, out32
+    q32 = I.barnes(tp, tv, sigma, x0, step, (W, H), num_iter=n, out_dtype=np.float64,
+                   precision="fp32c").cpu().numpy()
+    diff = np.isnan(q32) != np.isnan(ref_q)
+    assert np.all(np.abs(wg[diff] - thr) <= 1e-4 * abs(thr))
+    assert rel_err(q32, ref_q) <= 1e-5
 
 
 def test_batch_of_512_uneven_fields():
@@ -181,24 +223,11 @@ def test_3d_full_size_and_constant_field():
     q32 = I.barnes(tp, tv, sigma, (0, 0, 0), step, size, num_iter=4, out_dtype=np.float64, precision="fp32c")
     a, b = q32.cpu().numpy(), q64.cpu().numpy()
     assert rel_err(a, b) <= 1e-5
-    # FP64 against the oracle on the whole volume: the float64 quotient within
-    # 1e-9 of max(|ref|, range(val)); the float32 result within 1 ulp plus
-    # that float64 tolerance (the values cross zero, where a float32 ulp is
-    # far below it, and rounding two float64 values to float32 keeps them
-    # within their distance plus an ulp); masks equal but where the weight is
-    # within 1e-9 of the mask level
+    # FP64 against the oracle on the whole volume
     ref_out, ref_q, wg, thr = oracle.interpolate(pts, val, np.array(sigma), np.zeros(3), np.array(step), size, 4,
                                                  nthreads=16)
     out32 = I.barnes(tp, tv, sigma, (0, 0, 0), step, size, num_iter=4).cpu().numpy()
-    diff = np.isnan(b) != np.isnan(ref_q)
-    assert np.all(np.abs(wg[diff] - thr) <= 1e-9 * abs(thr))
-    m = ~np.isnan(b) & ~np.isnan(ref_q)
-    assert m.any()
-    scale = np.maximum(np.abs(ref_q[m]), np.ptp(val))
-    assert np.max(np.abs(b[m] - ref_q[m]) / scale) <= 1e-9
-    m32 = ~np.isnan(out32) & ~np.isnan(ref_out)
-    tol32 = np.spacing(np.abs(ref_out[m32])).astype(np.float64) + 1e-9 * np.maximum(np.abs(ref_q[m32]), np.ptp(val))
-    assert np.all(np.abs(out32[m32].astype(np.float64) - ref_out[m32]) <= tol32)
+    check_fp64_vs_oracle(b, out32, ref_out, ref_q, wg, thr, val)
     del ref_out, ref_q, wg, out32
     const = torch.full_like(tv, 7.25)
     for prec in ("fp64", "fp32c"):
