@@ -4,6 +4,9 @@
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
+#include <set>
+#include <utility>
 
 #include "fb_axis_impl.cuh"
 
@@ -49,18 +52,66 @@ static int col_g(int precision) { return (precision == 0 ? kColBytesF64 : kColBy
 int axis_col_group(int precision) { return col_g(precision); }
 constexpr int kMaxThreads = 512;
 
+// Per-device properties and kernel attributes.  A process may drive several
+// devices (and several host threads): the shared-memory opt-in limit and the
+// SM count are looked up once per device, and a kernel's dynamic
+// shared-memory attribute, which applies to one device only, is set once per
+// (kernel, device), all under one lock.
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_dev_mu;
+int g_smem_optin[kMaxDevices];
+int g_sm_count[kMaxDevices];
+std::set<std::pair<const void *, int>> g_attr_set;
+
+int cur_device()
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+        dev = 0;
+    return dev;
+}
+}  // namespace
+
 size_t axis_smem_limit()
 {
-    static int lim = -1;
-    if (lim < 0) {
-        int dev = 0, v = 0;
-        cudaGetDevice(&dev);
+    const int dev = cur_device();
+    std::lock_guard<std::mutex> lk(g_dev_mu);
+    if (g_smem_optin[dev] <= 0) {
+        int v = 0;
         if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess || v <= 0)
             v = 227 * 1024;
         // keep room for the kernels' few bytes of static shared memory
-        lim = v - 1024;
+        g_smem_optin[dev] = v - 1024;
     }
-    return (size_t)lim;
+    return (size_t)g_smem_optin[dev];
+}
+
+int device_sm_count()
+{
+    const int dev = cur_device();
+    std::lock_guard<std::mutex> lk(g_dev_mu);
+    if (g_sm_count[dev] <= 0) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
+            v = 1;
+        g_sm_count[dev] = v;
+    }
+    return g_sm_count[dev];
+}
+
+cudaError_t ensure_smem_attr(const void *func)
+{
+    const size_t lim = axis_smem_limit();
+    const int dev = cur_device();
+    std::lock_guard<std::mutex> lk(g_dev_mu);
+    const auto key = std::make_pair(func, dev);
+    if (g_attr_set.count(key))
+        return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim);
+    if (e == cudaSuccess)
+        g_attr_set.insert(key);
+    return e;
 }
 
 static int even(int64_t x) { return (int)((x + 1) / 2 * 2); }

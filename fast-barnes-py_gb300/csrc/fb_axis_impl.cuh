@@ -1094,7 +1094,6 @@ __global__ void __maxnreg__((AxisRegs<Real, K, MODE, LAYOUT>::value))
 // launch templates
 // ---------------------------------------------------------------------------
 
-size_t axis_smem_limit();
 int axis_threads(int precision, const AxisLaunch &a);
 
 template <typename Real, int K, int MODE, int SD, int LAY>
@@ -1102,14 +1101,9 @@ static cudaError_t launch_one(const AxisLaunch &a, const Geometry &g, const Samp
 {
     const int prec = sizeof(Real) == 8 ? 0 : 1;
     const size_t smem = axis_smem_bytes(prec, a);
-    static bool configured = false;
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_axis<Real, K, MODE, SD, LAY>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)axis_smem_limit());
-        if (e != cudaSuccess)
-            return e;
-        configured = true;
-    }
+    cudaError_t e = ensure_smem_attr((const void *)k_axis<Real, K, MODE, SD, LAY>);
+    if (e != cudaSuccess)
+        return e;
     const int64_t groups = a.layout == 0 ? (a.nlines + a.lines_per_cta - 1) / a.lines_per_cta
                                          : a.outer_count * a.xblocks;
     const int64_t blocks = groups * a.ntiles;
@@ -1145,8 +1139,7 @@ static cudaError_t launch_batch_one(int op, const AxisLaunch &a, const Geometry 
         k_axis_batch<Real, K, MODE, SD, LAY><<<grid2, threads, smem, st>>>(a, g, sv, fields, bpf);
         return cudaGetLastError();
     }
-    cudaError_t e = cudaFuncSetAttribute(k_axis_batch<Real, K, MODE, SD, LAY>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)axis_smem_limit());
+    cudaError_t e = ensure_smem_attr((const void *)k_axis_batch<Real, K, MODE, SD, LAY>);
     if (e != cudaSuccess)
         return e;
     *grid = (int)nitems;
@@ -1163,8 +1156,7 @@ static cudaError_t launch_mixed_one(int op, const MixedField *fields, const uint
         k_axis_mixed<Real, K, MODE, SD, LAY><<<nitems, threads, smem, st>>>(fields, items);
         return cudaGetLastError();
     }
-    return cudaFuncSetAttribute(k_axis_mixed<Real, K, MODE, SD, LAY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)axis_smem_limit());
+    return ensure_smem_attr((const void *)k_axis_mixed<Real, K, MODE, SD, LAY>);
 }
 
 template <typename Real, int K, int MODE>

@@ -1653,7 +1653,9 @@ std::mutex g_scratch_mu;
 double *g_scratch_ptr[kMaxScratchDevices] = {};
 
 // Address of the scratch array on the current device; the first call for a
-// device looks it up (no allocation).
+// device looks it up (no allocation).  The cached address stays valid for
+// the lifetime of the device's primary context (a cudaDeviceReset would
+// reload the module, possibly elsewhere).
 int resample_scratch(double **out)
 {
     int dev = -1;

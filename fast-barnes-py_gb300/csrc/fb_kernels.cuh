@@ -19,6 +19,13 @@ cudaError_t batch_sort(int precision, const BatchKeyField *d_fields, const uint2
                        uint32_t *bin_start, const uint32_t **sorted_idx, const void **recs, cudaStream_t st);
 
 // fb_axis.cu
+// Dynamic shared memory one block may opt into on the current device (less a
+// small reserve for static shared memory), and the device's SM count.
+size_t axis_smem_limit();
+int device_sm_count();
+// Sets a kernel's dynamic shared-memory limit to axis_smem_limit() on the
+// current device, once per (kernel, device); thread-safe.
+cudaError_t ensure_smem_attr(const void *func);
 struct AxisPlanLimits {
     int extent_max;        // longest line extent a rows-layout CTA holds
     int extent_max_cols;   // longest line extent a columns-layout CTA holds

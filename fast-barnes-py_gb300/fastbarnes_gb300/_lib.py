@@ -135,9 +135,6 @@ def version():
 # device plumbing (torch provides device memory and the current stream)
 # ---------------------------------------------------------------------------
 
-_ws_cache = {}
-
-
 def torch_cuda():
     import torch
     if not torch.cuda.is_available():
@@ -146,14 +143,16 @@ def torch_cuda():
 
 
 def workspace(nbytes, device):
-    """A cached uint8 device buffer of at least nbytes on `device`."""
+    """A uint8 device buffer of at least nbytes on `device` for one call.
+
+    Every call gets its own buffer from torch's caching allocator, which is
+    stream-ordered: a freed block is handed out again only to work on the
+    stream it was allocated on (after that stream's earlier work), so calls
+    from several host threads or on several torch streams never share
+    scratch memory.  After the first call of a size the allocation is a cache
+    hit (no cudaMalloc)."""
     torch = torch_cuda()
-    key = (device.index if device.index is not None else torch.cuda.current_device())
-    buf = _ws_cache.get(key)
-    if buf is None or buf.numel() < nbytes:
-        buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
-        _ws_cache[key] = buf
-    return buf
+    return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
 
 
 def stream_ptr(torch, device):

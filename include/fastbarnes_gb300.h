@@ -278,7 +278,10 @@ int fb_resample(const float *d_lam, int64_t lam_w, int64_t lam_h, const double *
  * a cudaMalloc / cudaFree would break).  The tables live in a static device
  * array of 49152 doubles (384 KiB), so size[1] + 2 * size[0] <= 49152; larger
  * grids return FB_ERR_ARG.  The first call on a device looks the array up
- * (cudaGetSymbolAddress) -- make it once before any stream capture.  Calls
+ * (cudaGetSymbolAddress) -- make it once before any stream capture -- and
+ * keeps the address for later calls on that device; the address is valid
+ * for the lifetime of the device's primary context, so a process that
+ * resets the device (cudaDeviceReset) must not call this entry again.  Calls
  * that overlap in time on one device share the array and race: serialize
  * them.  Allocates nothing. */
 int fb_resample_noalloc(const float *d_lam, int64_t lam_w, int64_t lam_h, const double *lam_x0, const double *x0,

@@ -146,6 +146,40 @@ FBO_EXPORT double *fbo_accumulate_array(double *in_arr, double *h_arr, int arr_l
     return in_arr;
 }
 
+/* Not a restatement: the same num_iter passes as fbo_accumulate_tail_array,
+ * but every output summed directly over its window (2T + 1 cells plus the
+ * two tails, zero outside [0, arr_len)), so no rounding is carried from one
+ * output to the next.  The reference's running sum carries its rounding along
+ * the whole line; on very long lines this direct form is the more accurate
+ * float64 value of the same quantity and serves as the truth both are
+ * measured against.  Cells run in parallel (nthreads). */
+FBO_EXPORT double *fbo_direct_tail_passes(double *in_arr, double *h_arr, int64_t arr_len, int rect_len,
+                                          int num_iter, double alpha, int nthreads)
+{
+    const int64_t T = (rect_len - 1) / 2;
+    (void)nthreads;
+    for (int it = 0; it < num_iter; it++) {
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+        for (int64_t k = 0; k < arr_len; k++) {
+            const int64_t lo = k - T < 0 ? 0 : k - T;
+            const int64_t hi = k + T > arr_len - 1 ? arr_len - 1 : k + T;
+            double acc = 0.0;
+            for (int64_t m = lo; m <= hi; m++)
+                acc += in_arr[m];
+            double tails = 0.0;
+            if (k - T - 1 >= 0)
+                tails += in_arr[k - T - 1];
+            if (k + T + 1 < arr_len)
+                tails += in_arr[k + T + 1];
+            h_arr[k] = acc + alpha * tails;
+        }
+        double *t = in_arr;
+        in_arr = h_arr;
+        h_arr = t;
+    }
+    return in_arr;
+}
+
 /* ------------------------------------------------------------------------- */
 /* splat                                                                      */
 /* ------------------------------------------------------------------------- */
@@ -216,13 +250,30 @@ static void inject(int dim, double *vg, double *wg, const double *pts, const dou
  * _convolve_{1,2,3}d (:617-724).  Lines are gathered with their stride, as the
  * reference's .copy() does, and written back. */
 static void convolve_axis(double *f, const int64_t *shape_xyz, int axis, int rect_len,
-                          int num_iter, double alpha, int tail, int nthreads)
+                          int num_iter, double alpha, int tail, int nthreads, int direct)
 {
     int64_t W = shape_xyz[0], H = shape_xyz[1], D = shape_xyz[2];
     int64_t len = axis == 0 ? W : (axis == 1 ? H : D);
     int64_t stride = axis == 0 ? 1 : (axis == 1 ? W : W * H);
     int64_t nlines = (W * H * D) / len;
     (void)nthreads;
+    if (direct) {
+        /* the drift-free truth (test use): lines one after another, the
+         * cells of a line in parallel */
+        double *a = (double *)malloc(sizeof(double) * len);
+        double *h = (double *)malloc(sizeof(double) * len);
+        for (int64_t li = 0; li < nlines; li++) {
+            int64_t base = axis == 0 ? li * W : (axis == 1 ? (li / W) * W * H + li % W : li);
+            for (int64_t k = 0; k < len; k++)
+                a[k] = f[base + k * stride];
+            double *r = fbo_direct_tail_passes(a, h, len, rect_len, num_iter, tail ? alpha : 0.0, nthreads);
+            for (int64_t k = 0; k < len; k++)
+                f[base + k * stride] = r[k];
+        }
+        free(a);
+        free(h);
+        return;
+    }
 #pragma omp parallel num_threads(nthreads)
     {
         double *a = (double *)malloc(sizeof(double) * len);
@@ -257,11 +308,38 @@ static void convolve_axis(double *f, const int64_t *shape_xyz, int axis, int rec
  *   q64     : optional, the float64 quotient before the float32 cast
  *   wg_out  : optional, the convolved weight field before the NaN mask
  * Returns the NaN threshold applied to the weight field. */
+static double interpolate_impl(int method, int dim, const double *pts, const double *val, int64_t npts,
+                               const double *sigma, const double *x0, const double *step, const int64_t *size,
+                               int num_iter, double max_dist_weight, int nthreads, float *out_f32, double *q64,
+                               double *wg_out, int direct);
+
 FBO_EXPORT double fbo_interpolate(int method, int dim, const double *pts, const double *val,
                                   int64_t npts, const double *sigma, const double *x0,
                                   const double *step, const int64_t *size, int num_iter,
                                   double max_dist_weight, int nthreads, float *out_f32,
                                   double *q64, double *wg_out)
+{
+    return interpolate_impl(method, dim, pts, val, npts, sigma, x0, step, size, num_iter, max_dist_weight,
+                            nthreads, out_f32, q64, wg_out, 0);
+}
+
+/* Not a restatement: fbo_interpolate with every pass summed directly over its
+ * window (fbo_direct_tail_passes) instead of the reference's running sums --
+ * the drift-free float64 truth for very long lines. */
+FBO_EXPORT double fbo_interpolate_direct(int method, int dim, const double *pts, const double *val,
+                                         int64_t npts, const double *sigma, const double *x0,
+                                         const double *step, const int64_t *size, int num_iter,
+                                         double max_dist_weight, int nthreads, float *out_f32,
+                                         double *q64, double *wg_out)
+{
+    return interpolate_impl(method, dim, pts, val, npts, sigma, x0, step, size, num_iter, max_dist_weight,
+                            nthreads, out_f32, q64, wg_out, 1);
+}
+
+static double interpolate_impl(int method, int dim, const double *pts, const double *val, int64_t npts,
+                               const double *sigma, const double *x0, const double *step, const int64_t *size,
+                               int num_iter, double max_dist_weight, int nthreads, float *out_f32, double *q64,
+                               double *wg_out, int direct)
 {
     int64_t shp[3] = {size[0], dim > 1 ? size[1] : 1, dim > 2 ? size[2] : 1};
     int64_t total = shp[0] * shp[1] * shp[2];
@@ -295,8 +373,8 @@ FBO_EXPORT double fbo_interpolate(int method, int dim, const double *pts, const 
             alpha = 0.0;
         }
         ks = 2 * hks + 1;
-        convolve_axis(vg, shp, m, ks, num_iter, alpha, method == 0, nthreads);
-        convolve_axis(wg, shp, m, ks, num_iter, alpha, method == 0, nthreads);
+        convolve_axis(vg, shp, m, ks, num_iter, alpha, method == 0, nthreads, direct);
+        convolve_axis(wg, shp, m, ks, num_iter, alpha, method == 0, nthreads, direct);
         /* interpolation.py:424 / :669.  The plain method raises the int32
          * kernel size to the power n in int32 arithmetic, which wraps around
          * for large kernels; the product is reproduced modulo 2^32. */

@@ -53,6 +53,8 @@ def lib():
         L.fbo_accumulate_array.restype = P
         L.fbo_interpolate.argtypes = [i, i, P, P, i64, P, P, P, P, i, d, i, P, P, P]
         L.fbo_interpolate.restype = d
+        L.fbo_interpolate_direct.argtypes = [i, i, P, P, i64, P, P, P, P, i, d, i, P, P, P]
+        L.fbo_interpolate_direct.restype = d
         L.fbo_interpolate_naive.argtypes = [i, P, P, i64, P, P, P, P, i, P]
         L.fbo_interpolate_naive.restype = None
         L.fbo_interpolate_naive_s2.argtypes = [P, P, i64, P, P, P, P, i, P]
@@ -108,10 +110,15 @@ def _vec(x, dim, dtype=np.float64):
 
 
 def interpolate(pts, val, sigma, x0, step, size, num_iter=4, max_dist=3.5,
-                method="optimized_convolution", nthreads=1):
+                method="optimized_convolution", nthreads=1, direct=False):
     """Returns (out_f32, q64, wg, thr) exactly as the reference computes them:
     out_f32 is barnes()'s return value, q64 the float64 quotient before the
-    cast, wg the convolved weights before the NaN mask, thr the mask level."""
+    cast, wg the convolved weights before the NaN mask, thr the mask level.
+
+    direct=True computes every box pass by summing each output's window
+    directly instead of the reference's running sums (fbo_direct_tail_passes):
+    not the reference's rounding, but the drift-free float64 value of the
+    same quantity, used as the truth on very long lines."""
     pts = np.asarray(pts, np.float64)
     if pts.ndim == 1:
         pts = pts.reshape(-1, 1)
@@ -125,7 +132,8 @@ def interpolate(pts, val, sigma, x0, step, size, num_iter=4, max_dist=3.5,
     wg = np.empty(shape, np.float64)
     m = 0 if method == "optimized_convolution" else 1
     mdw = math.exp(-max_dist ** 2 / 2)
-    thr = lib().fbo_interpolate(m, dim, _p(pts), _p(val), len(val), _p(_vec(sigma, dim)),
+    fn = lib().fbo_interpolate_direct if direct else lib().fbo_interpolate
+    thr = fn(m, dim, _p(pts), _p(val), len(val), _p(_vec(sigma, dim)),
                                 _p(_vec(x0, dim)), _p(_vec(step, dim)), _p(sz), int(num_iter),
                                 mdw, int(nthreads), _p(out), _p(q), _p(wg))
     return out, q, wg, thr

@@ -1,7 +1,8 @@
 """Generate the golden fixtures in tests/golden/ by running the reference itself.
 
-This script imports MeteoSwiss/fast-barnes-py from a source checkout (default
-/root/reference, override with FASTBARNES_REF) as plain Python/NumPy: numba is
+This script imports MeteoSwiss/fast-barnes-py from a source checkout, given
+as the FASTBARNES_REF environment variable or the --ref DIR argument (there is
+no default location), as plain Python/NumPy: numba is
 not installed here, so a stub ``numba`` module whose ``njit`` returns the
 function unchanged is put in ``sys.modules`` first.  With ``fastmath`` off (the
 numba default the reference uses) the jitted loops are scalar IEEE float64
@@ -32,10 +33,32 @@ from math import exp
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("FASTBARNES_REF", "/root/reference")
+
+
+def _reference_dir():
+    """The reference checkout: --ref DIR on the command line, else the
+    FASTBARNES_REF environment variable; no default."""
+    argv = sys.argv[1:]
+    if "--ref" in argv:
+        i = argv.index("--ref")
+        if i + 1 >= len(argv):
+            raise SystemExit("--ref needs a directory")
+        ref = argv[i + 1]
+        del sys.argv[i + 1:i + 3]
+        return ref
+    ref = os.environ.get("FASTBARNES_REF")
+    if not ref:
+        raise SystemExit("set FASTBARNES_REF or pass --ref DIR (a MeteoSwiss/fast-barnes-py source checkout)")
+    return ref
+
+
+REF = None
 
 
 def import_reference():
+    global REF
+    if REF is None:
+        REF = _reference_dir()
     if "numba" not in sys.modules:
         stub = types.ModuleType("numba")
 
