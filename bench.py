@@ -268,7 +268,8 @@ def main():
     ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--knobs", default="", help="pin the launch shape 'chunk,rows_threads' instead of tuning")
+    ap.add_argument("--knobs", default="",
+                    help="pin the launch shape 'chunk,rows_threads[,mixed[,cols_pipe]]' instead of tuning")
     ap.add_argument("--quick", action="store_true",
                     help="warm-up and timed steps only (no fp64 form, e2e or CPU baseline): for profiler runs")
     args = ap.parse_args()
@@ -591,7 +592,8 @@ def main():
                 "config": workload_config(B, args.precision) | {"parallelism": f"replicas x{world}",
                                                                  "knobs": {"chunk": knobs[0],
                                                                            "rows_threads": knobs[1],
-                                                                           "mixed": knobs[2]}},
+                                                                           "mixed": knobs[2],
+                                                                           "cols_pipe": knobs[3]}},
                 "gpu_launches": launches_per_step * args.steps,
                 "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
                              "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,

@@ -22,7 +22,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=o
 # per-file extra flags: the sphere projection keeps separate multiply / add
 EXTRA = {"fb_s2.cu": ["-fmad=false"]}
 SOURCES = ["fb_sort.cu", "fb_axis.cu", "fb_axis_f32.cu", "fb_axis_f32l.cu", "fb_axis_f64.cu", "fb_axis_f64s.cu",
-           "fb_s2.cu", "fb_grad.cu", "fb_naive.cu", "fb_capi.cu"]
+           "fb_cols.cu", "fb_cols_f32.cu", "fb_cols_f64.cu", "fb_s2.cu", "fb_grad.cu", "fb_naive.cu", "fb_capi.cu"]
 
 
 def nvcc():

@@ -263,6 +263,21 @@ cudaError_t launch_axis(int precision, const AxisLaunch &a, const Geometry &g, c
     const int sd = a.fill_splat ? g.dim : 0;
     if (a.layout == 1 && a.fill_splat)
         return cudaErrorInvalidValue;
+    if (a.layout == 1) {
+        ColsPipe cp;
+        int k = 0, mode = 0;
+        CUtensorMap map;
+        if (cols_pipe_plan(precision, a, g, 1, cp, k, mode) &&
+            cols_pipe_map(precision, cp, g, a.src_v, 0, 1, &map) == cudaSuccess) {
+            cp.single.src = a.src_v;
+            cp.single.dst = a.dst_v;
+            cp.single.out = a.out;
+            cp.single.bin_start = sv.bin_start;
+            cp.single.hdr = sv.hdr;
+            cp.status = sv.hdr ? reinterpret_cast<uint32_t *>(const_cast<int *>(&sv.hdr->error)) : nullptr;
+            return launch_cols_pipe(precision, k, mode, map, cp, nullptr, st);
+        }
+    }
     const int mode = direct_mode(precision, a.T) ? 1 : 0;
     if (precision == 0)
         return launch_axis_f64(kchunk_of(precision, a.T, a.kchunk), mode, sd, a, g, sv, st);
@@ -275,6 +290,8 @@ int axis_tune(const char *name, int value)
         g_chunk_choice = value;
         return 0;
     }
+    if (strcmp(name, "cols_pipe") == 0)
+        return cols_pipe_tune(value);
     return -1;
 }
 

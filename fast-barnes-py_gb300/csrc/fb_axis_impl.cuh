@@ -134,6 +134,72 @@ __device__ __forceinline__ void bulk_store(void *gmem, const void *smem, unsigne
 __device__ __forceinline__ void bulk_store_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory"); }
 
 // ---------------------------------------------------------------------------
+// mbarriers and bulk loads (tensor memory accelerator)
+// ---------------------------------------------------------------------------
+
+constexpr uint64_t kWaitLimitNs = 1000000000ull;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t global_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t a, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t a, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t a, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.b32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Waits for the phase of parity `parity` to complete; false after
+// kWaitLimitNs without completion.
+__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity)
+{
+    if (mbar_try_wait(a, parity))
+        return true;
+    const uint64_t t0 = global_ns();
+    for (uint32_t n = 1;; n++) {
+        if (mbar_try_wait(a, parity))
+            return true;
+        if ((n & 63u) == 0u && global_ns() - t0 > kWaitLimitNs)
+            return false;
+    }
+}
+
+// Bulk copy of `bytes` (a multiple of 16, both addresses 16-byte aligned)
+// from global to shared memory, completing on mbarrier `mbar`.
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void *src, uint32_t bytes, uint32_t mbar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(mbar)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t a)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(a) : "memory");
+}
+// Orders this thread's generic-proxy shared-memory accesses before later
+// async-proxy (TMA) accesses of the same memory.
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// ---------------------------------------------------------------------------
 // one line seen by one thread: cell e lives at s[e * ES]; the line buffer has
 // zero cells on both sides (T + 1 before the line, up to the end of the last
 // chunk + T + 1 after it), so no read needs a bounds check
@@ -873,16 +939,15 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
             }
             __syncthreads();
             if (active) {
-                if (!edge_warp) {
+                // Unchecked: outputs outside [0, E) were cleared above, and
+                // every chunk position, -(T + 1) .. nact * K - 1, lies inside
+                // the line buffer (its zero pads), so writing those zeros
+                // back keeps the pads zero.  (A checked write-back in the
+                // warps holding edge chunks made every other warp wait for
+                // them at the next barrier.)
 #pragma unroll
-                    for (int i = 0; i < K; i++)
-                        ln[(a0 + i) * ES] = o[i];
-                } else {
-#pragma unroll
-                    for (int i = 0; i < K; i++)
-                        if (a0 + i >= 0 && a0 + i < E)
-                            ln[(a0 + i) * ES] = o[i];
-                }
+                for (int i = 0; i < K; i++)
+                    ln[(a0 + i) * ES] = o[i];
                 if (more) {
                     pw[0] = own_s;
                     pw[QS] = X;

@@ -5,6 +5,7 @@
 // expressions operation by operation; this file is compiled without FMA
 // contraction so the host results are identical on x86 and aarch64.
 #include <math.h>
+#include <stddef.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <string.h>
@@ -35,6 +36,14 @@ static int fail(int code, const char *fmt, ...)
 static int cuda_fail(cudaError_t e, const char *where)
 {
     return fail(FB_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
+}
+
+// FB_ERR_DEVICE with a message naming the status bits a kernel recorded.
+static int device_fail(uint32_t bits, const char *where)
+{
+    return fail(FB_ERR_DEVICE, "%s: device status 0x%x%s%s", where, bits,
+                (bits & FB_DEVICE_TIMEOUT) ? " (a pipeline wait ran out: the kernel stopped early)" : "",
+                (bits & FB_DEVICE_BOUNDS) ? " (an out-of-range index was skipped: bounds-check build)" : "");
 }
 
 extern "C" const char *fb_version(void) { return "fastbarnes_gb300 0.1 (sm_103a)"; }
@@ -719,11 +728,35 @@ extern "C" int fb_interpolate_host(int method, int precision, int dim, const dou
     if (rc != FB_OK)
         return rc;
     e = cudaMemcpyAsync(out, d_out, out_b, cudaMemcpyDeviceToHost, st);
+    int status = 0;
+    if (e == cudaSuccess && !p.naive)
+        e = cudaMemcpyAsync(&status, ws + p.off_hdr + offsetof(FieldHeader, error), sizeof(int),
+                            cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(st);
     if (e != cudaSuccess)
         return cuda_fail(e, "copy to host");
+    if (status != 0)
+        return device_fail((uint32_t)status, "fb_interpolate_host");
     return FB_OK;
+}
+
+extern "C" int fb_workspace_status(const void *d_workspace, void *stream, int *status)
+{
+    g_err[0] = 0;
+    if (!d_workspace)
+        return fail(FB_ERR_ARG, "null workspace");
+    int bits = 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaMemcpyAsync(&bits, static_cast<const char *>(d_workspace) + offsetof(FieldHeader, error),
+                                    sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "fb_workspace_status");
+    if (status)
+        *status = bits;
+    return bits ? device_fail((uint32_t)bits, "fb_workspace_status") : FB_OK;
 }
 
 extern "C" void *fb_host_alloc(size_t bytes)
@@ -966,6 +999,11 @@ struct BatchStage {
     size_t off_fields = 0;    // TilePtrs[nf] (homogeneous) or MixedField[nf] (mixed)
     size_t off_items = 0;     // mixed: uint2 (field, block)[nitems]
     uint32_t nf = 0, bpf = 0, nitems = 0;
+    // homogeneous column stages of whole lines: the pipelined TMA kernel
+    bool pipe = false;
+    int pk = 0, pmode = 0;
+    ColsPipe cp{};
+    CUtensorMap map{};
 };
 
 bool same_launch(const AxisLaunch &x, const AxisLaunch &y)
@@ -1057,6 +1095,8 @@ int batch_build(int precision, const fb_field2d *fields, int nf, int out_f64, fb
         return fail(FB_ERR_ARG, "rows_threads must be 0, 128, 256 or 512 (got %d)", kn.rows_threads);
     if (kn.mixed != 0 && kn.mixed != 1)
         return fail(FB_ERR_ARG, "mixed must be 0 or 1 (got %d)", kn.mixed);
+    if (kn.cols_pipe < 0 || kn.cols_pipe > 2)
+        return fail(FB_ERR_ARG, "cols_pipe must be 0, 1 or 2 (got %d)", kn.cols_pipe);
     b->precision = precision;
     b->out_f64 = out_f64 ? 1 : 0;
     b->knobs = kn;
@@ -1298,6 +1338,24 @@ int batch_build(int precision, const fb_field2d *fields, int nf, int out_f64, fb
             st.a.out_f64 = b->out_f64;
             st.sv = view(g.f[0]);
             e = launch_axis_batch(0, precision, st.a, st.g, st.sv, nullptr, st.bpf, st.nitems, &st.grid, nullptr);
+            // column stages: the pipelined kernel when the fields' source
+            // cells are evenly spaced (one tensor map over all of them)
+            if (e == cudaSuccess && st.a.layout == 1 &&
+                cols_pipe_plan(precision, st.a, st.g, (int)g.f.size(), st.cp, st.pk, st.pmode,
+                               kn.cols_pipe == 0 ? -1 : (kn.cols_pipe == 1 ? 1 : 0))) {
+                const char *s0 = static_cast<const char *>(tp[0].src);
+                const int64_t fstride = g.f.size() > 1 ? static_cast<const char *>(tp[1].src) - s0 : 0;
+                bool even = fstride >= 0 && fstride % 16 == 0;
+                for (size_t mi = 1; even && mi < g.f.size(); mi++)
+                    even = static_cast<const char *>(tp[mi].src) == s0 + (int64_t)mi * fstride;
+                if (even &&
+                    cols_pipe_map(precision, st.cp, st.g, s0, fstride, (int)g.f.size(), &st.map) == cudaSuccess) {
+                    st.pipe = true;
+                    st.cp.status =
+                        reinterpret_cast<uint32_t *>(&reinterpret_cast<FieldHeader *>(dv + b->off_hdrs)->error);
+                    st.grid = st.cp.ntiles > 0 ? 1 : 0;
+                }
+            }
         }
         if (e != cudaSuccess)
             return cuda_fail(e, "batch axis kernel setup");
@@ -1330,7 +1388,10 @@ int batch_enqueue(fb_batch *b, cudaStream_t st, bool prof)
     }
     for (size_t i = 0; i < b->stages.size(); i++) {
         BatchStage &s = b->stages[i];
-        if (s.mixed)
+        if (s.pipe)
+            e = launch_cols_pipe(b->precision, s.pk, s.pmode, s.map, s.cp,
+                                 reinterpret_cast<const TilePtrs *>(dv + s.off_fields), st);
+        else if (s.mixed)
             e = launch_axis_mixed(1, b->precision, s.k, s.mode, s.sd, s.layout,
                                   reinterpret_cast<const MixedField *>(dv + s.off_fields),
                                   reinterpret_cast<const uint2 *>(dv + s.off_items), s.nitems, s.smem, s.threads,
@@ -1386,40 +1447,46 @@ int batch_tune(int precision, const fb_field2d *fields, int nf, int out_f64, fb_
     if (e == cudaSuccess)
         e = cudaEventCreate(&e1);
     float best_ms = 1e30f;
-    *best = fb_batch_knobs{0, 0, 0};
+    *best = fb_batch_knobs{0, 0, 0, 0};
     int rc = e == cudaSuccess ? FB_OK : cuda_fail(e, "tuning stream");
-    for (int c : chunks) {
-        for (int r : rows) {
-          for (int mx : mixes) {
-            if (rc != FB_OK)
-                break;
-            fb_batch tb;
-            rc = batch_build(precision, fields, nf, out_f64, fb_batch_knobs{c, r, mx}, &tb);
-            float t_best = 1e30f;
-            for (int it = 0; rc == FB_OK && it < 7; it++) {
-                if (it >= 2)
-                    cudaEventRecord(e0, st);
-                rc = batch_enqueue(&tb, st, false);
-                if (rc == FB_OK && it >= 2) {
-                    cudaEventRecord(e1, st);
-                    e = cudaEventSynchronize(e1);
-                    float ms = 0.f;
-                    if (e == cudaSuccess)
-                        e = cudaEventElapsedTime(&ms, e0, e1);
-                    if (e != cudaSuccess)
-                        rc = cuda_fail(e, "tuning run");
-                    t_best = std::min(t_best, ms);
-                }
+    // best of 5 timed runs (after 2 warm-up runs) of one candidate
+    auto try_knobs = [&](fb_batch_knobs kn) {
+        if (rc != FB_OK)
+            return;
+        fb_batch tb;
+        rc = batch_build(precision, fields, nf, out_f64, kn, &tb);
+        float t_best = 1e30f;
+        for (int it = 0; rc == FB_OK && it < 7; it++) {
+            if (it >= 2)
+                cudaEventRecord(e0, st);
+            rc = batch_enqueue(&tb, st, false);
+            if (rc == FB_OK && it >= 2) {
+                cudaEventRecord(e1, st);
+                e = cudaEventSynchronize(e1);
+                float ms = 0.f;
+                if (e == cudaSuccess)
+                    e = cudaEventElapsedTime(&ms, e0, e1);
+                if (e != cudaSuccess)
+                    rc = cuda_fail(e, "tuning run");
+                t_best = std::min(t_best, ms);
             }
-            if (rc == FB_OK && t_best < best_ms) {
-                best_ms = t_best;
-                *best = fb_batch_knobs{c, r, mx};
-            }
-            cudaStreamSynchronize(st);
-            batch_free(&tb);
-          }
         }
-    }
+        if (rc == FB_OK && t_best < best_ms) {
+            best_ms = t_best;
+            *best = kn;
+        }
+        cudaStreamSynchronize(st);
+        batch_free(&tb);
+    };
+    for (int c : chunks)
+        for (int r : rows)
+            for (int mx : mixes)
+                try_knobs(fb_batch_knobs{c, r, mx, 0});
+    // then the column kernel, both ways, on the best launch shape
+    const fb_batch_knobs shape = *best;
+    if (!shape.mixed)
+        for (int pipe = 1; pipe <= 2; pipe++)
+            try_knobs(fb_batch_knobs{shape.chunk, shape.rows_threads, 0, pipe});
     if (e0)
         cudaEventDestroy(e0);
     if (e1)
@@ -1596,6 +1663,27 @@ extern "C" int fb_batch_knobs_of(const fb_batch *b, fb_batch_knobs *knobs)
         return fail(FB_ERR_ARG, "null argument");
     *knobs = b->knobs;
     return FB_OK;
+}
+
+extern "C" int fb_batch_status(const fb_batch *b, void *stream, int *status)
+{
+    g_err[0] = 0;
+    if (!b)
+        return fail(FB_ERR_ARG, "null plan");
+    std::vector<FieldHeader> h((size_t)b->nfields);
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaMemcpyAsync(h.data(), b->dev + b->off_hdrs, sizeof(FieldHeader) * h.size(),
+                                    cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "fb_batch_status");
+    int bits = 0;
+    for (const FieldHeader &x : h)
+        bits |= x.error;
+    if (status)
+        *status = bits;
+    return bits ? device_fail((uint32_t)bits, "fb_batch_status") : FB_OK;
 }
 
 extern "C" int fb_batch_info(const fb_batch *b, int *kernel_launches, int *memsets, size_t *device_bytes)

@@ -7,6 +7,7 @@
 //   workspace: FieldHeader | bin keys | sort ping-pong | tile histograms |
 //              bin starts | two intermediate value/weight field pairs
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
@@ -227,6 +228,34 @@ struct MixedField {
     Geometry g;
     SampleView sv;
     TilePtrs fp;
+};
+
+// Device status word bits (FieldHeader::error of a field, or of the first
+// field of a batch): set by kernels that stop early instead of waiting on.
+constexpr uint32_t FB_DEVICE_TIMEOUT = 1u;   // a pipeline wait ran out
+constexpr uint32_t FB_DEVICE_BOUNDS = 2u;    // bounds-check build: an out-of-range index was skipped
+
+// Launch description of the pipelined columns kernel (fb_cols.cuh),
+// host-computed.
+struct ColsPipe {
+    int L;               // cells per line = rows of a tile
+    int line_pad;        // zero rows before row 0 of a stage (multiple of 4: 128-byte aligned boxes)
+    int line_pitch;      // rows per stage buffer
+    int chunks_pad;      // chunk slots per line
+    int part_pad, part_pitch;
+    int box_rows, nboxes;
+    int axis;            // 1: the lines run along y; 2: along z
+    int T, passes, scaled, store_quot, out_f64, quant_bits;
+    double alpha, inv_norm, thr;
+    uint32_t ntiles, tiles_per_field, xblocks;
+    int64_t width;           // lines per plane (grid x extent)
+    int64_t elem_stride;     // HBM cells between consecutive cells of a line
+    int64_t outer_stride;    // HBM cells between planes
+    uint32_t stage_bytes;    // one stage buffer (multiple of 128)
+    uint32_t part_bytes;     // one group's two partial-sum arrays (multiple of 128)
+    int nstages, ngroups, group_threads;
+    uint32_t *status;        // device status word (or null)
+    TilePtrs single;         // the field's pointers when `fields` is null (one field)
 };
 
 }  // namespace fbg

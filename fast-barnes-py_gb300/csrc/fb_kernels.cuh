@@ -63,6 +63,22 @@ int axis_tune(const char *name, int value);
 cudaError_t launch_lines(int precision, void *data, int64_t nlines, int64_t len, int T, double alpha,
                          int passes, int normalize, cudaStream_t st);
 
+// fb_cols.cu: the pipelined columns kernel (whole lines of the y / z axis,
+// TMA loads).  cols_pipe_plan fills the launch description for `nfields`
+// fields of one shape and returns false when the kernel does not apply (tiled
+// lines, splat fills, rows that are not a multiple of 16 bytes, or too little
+// shared memory / registers); cols_pipe_map encodes the tensor map over the
+// fields' source cells (field f at src0 + f * field_stride bytes).
+// cols_pipe_tune: 0 off, 1 on, 2 automatic (the default: by precision);
+// want: -1 follow that setting, 0 never, 1 wherever the kernel applies.
+int cols_pipe_tune(int value);
+bool cols_pipe_plan(int precision, const AxisLaunch &a, const Geometry &g, int nfields, ColsPipe &cp, int &K,
+                    int &mode, int want = -1);
+cudaError_t cols_pipe_map(int precision, const ColsPipe &cp, const Geometry &g, const void *src0,
+                          int64_t field_stride, int nfields, CUtensorMap *map);
+cudaError_t launch_cols_pipe(int precision, int k, int mode, const CUtensorMap &map, const ColsPipe &cp,
+                             const TilePtrs *fields, cudaStream_t st);
+
 // fb_grad.cu: seed (dL/dV, dL/dW) from dL/df in place over the final cells;
 // gather the adjoint cells at every sample's corners.
 cudaError_t launch_grad_seed(int precision, void *cells, int64_t npoints, const void *grad, int grad_f64, double thr,

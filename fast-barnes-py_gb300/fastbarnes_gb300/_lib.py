@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libfastbarnes_gb300.so")
 
 FB_OK = 0
-FB_ERR_ARG, FB_ERR_KERNEL_SIZE, FB_ERR_WORKSPACE, FB_ERR_CUDA, FB_ERR_UNSUPPORTED = 1, 2, 3, 4, 5
+FB_ERR_ARG, FB_ERR_KERNEL_SIZE, FB_ERR_WORKSPACE, FB_ERR_CUDA, FB_ERR_UNSUPPORTED, FB_ERR_DEVICE = 1, 2, 3, 4, 5, 6
 FB_FP64, FB_FP32C = 0, 1
 FB_OPTIMIZED_CONVOLUTION, FB_CONVOLUTION, FB_NAIVE = 0, 1, 2
 
@@ -42,7 +42,8 @@ class Field2D(ctypes.Structure):
 
 class BatchKnobs(ctypes.Structure):
     """fb_batch_knobs: launch shape of a batch plan."""
-    _fields_ = [("chunk", ctypes.c_int), ("rows_threads", ctypes.c_int), ("mixed", ctypes.c_int)]
+    _fields_ = [("chunk", ctypes.c_int), ("rows_threads", ctypes.c_int), ("mixed", ctypes.c_int),
+                ("cols_pipe", ctypes.c_int)]
 
 
 FB_BATCH_GRAPH, FB_BATCH_TUNE = 1, 2
@@ -110,6 +111,8 @@ def lib():
             "fb_batch_run_host": ([P, P, P, P, P], i),
             "fb_batch_enqueue_host": ([P, P, P, P, P], i),
             "fb_batch_knobs_of": ([P, ctypes.POINTER(BatchKnobs)], i),
+            "fb_batch_status": ([P, P, ctypes.POINTER(i)], i),
+            "fb_workspace_status": ([P, P, ctypes.POINTER(i)], i),
             "fb_batch_info": ([P, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(sz)], i),
             "fb_batch_destroy": ([P], None),
         }

@@ -126,6 +126,16 @@ int fb_interpolate_grad(int method, int precision, int dim, const double *d_pts,
                         int grad_f64, double *d_grad_val, double *d_grad_pts, void *d_workspace,
                         size_t workspace_bytes, void *stream);
 
+/* No reference counterpart: the device status word of a workspace after a
+ * call on `stream` (synchronizes the stream).  Kernels that stop early
+ * instead of waiting on (a pipeline wait that ran out), and, in the
+ * bounds-check build, kernels that skipped an out-of-range index, record a
+ * bit there: 1 = a wait ran out, 2 = an index was skipped.  Returns FB_OK
+ * and *status = 0 when the call ran to completion, else FB_ERR_DEVICE with
+ * the bits in *status.  The word is cleared at the start of every call that
+ * uses the workspace.  fb_interpolate_host checks it itself. */
+int fb_workspace_status(const void *d_workspace, void *stream, int *status);
+
 /* Pinned host memory for fb_interpolate_host buffers. */
 void *fb_host_alloc(size_t bytes);
 void fb_host_free(void *p);
@@ -182,6 +192,8 @@ typedef struct fb_batch_knobs {
     int chunk;                /* 0 automatic, 17 or 33 (float32 windows wider than 65) */
     int rows_threads;         /* x-axis threads per CTA target: 0 (= 128), 128, 256 or 512 */
     int mixed;                /* 1: per-field descriptions even when the fields share one shape */
+    int cols_pipe;            /* column stages: 0 library default for the precision, 1 the persistent
+                                 TMA-pipelined kernel where it applies, 2 one CTA per column group */
 } fb_batch_knobs;
 
 typedef struct fb_batch fb_batch;
@@ -204,6 +216,9 @@ int fb_batch_run_host(fb_batch *plan, const double *const *h_pts, const double *
 int fb_batch_enqueue_host(fb_batch *plan, const double *const *h_pts, const double *const *h_val,
                           void *const *h_out, void *stream);
 int fb_batch_knobs_of(const fb_batch *plan, fb_batch_knobs *knobs);
+/* The device status words of a plan's last run on `stream` (synchronizes
+ * it), ORed over the fields: as fb_workspace_status. */
+int fb_batch_status(const fb_batch *plan, void *stream, int *status);
 /* Kernel launches and memsets one fb_batch_run enqueues, and the plan's
  * device bytes. */
 int fb_batch_info(const fb_batch *plan, int *kernel_launches, int *memsets, size_t *device_bytes);
