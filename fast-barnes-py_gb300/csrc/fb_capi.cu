@@ -1242,7 +1242,13 @@ int batch_build(int precision, const fb_field2d *fields, int nf, int out_f64, fb
     cudaError_t e = cudaGetDevice(&b->device);
     if (e == cudaSuccess)
         e = cudaMalloc(&b->dev, b->dev_bytes);
+    // zeroed once: the bin counts and tickets of the sort are kept zero
+    // between runs by the kernels that consume them
+    if (e == cudaSuccess)
+        e = cudaMemset(b->dev, 0, b->dev_bytes);
     if (e != cudaSuccess) {
+        if (b->dev)
+            cudaFree(b->dev);
         b->dev = nullptr;
         return cuda_fail(e, "batch plan memory");
     }
@@ -1690,19 +1696,21 @@ extern "C" int fb_batch_info(const fb_batch *b, int *kernel_launches, int *memse
 {
     if (!b)
         return fail(FB_ERR_ARG, "null plan");
-    // batch_sort: k_batch_keys (when there are samples), the bin-start scan
-    // (one launch, or k_tile_sums, k_scan_exclusive and k_tile_scan for many
-    // bins), then k_bin_scatter, k_sort_bins and k_sort_large (which also put
-    // the records in sorted order) when there are samples, and two memsets;
-    // then one axis launch per stage with work
-    const int scans = (int64_t)b->nbins + 1 <= kOneBlockScanMax ? 1 : 3;
-    int k = scans + (b->nblocks > 0 ? 1 : 0) + (b->ntot > 0 ? 3 : 0);
+    // batch_sort: k_batch_keys with the bin-start scan in its last block
+    // (fused), or k_batch_keys and a separate scan (one launch, or
+    // k_tile_sums, k_scan_exclusive and k_tile_scan for many bins) and a
+    // memset of the counts; then k_bin_scatter and k_sort_bins (which also
+    // puts the records in sorted order) when there are samples; a memset of
+    // the field headers; then one axis launch per stage with work
+    const bool fused = batch_sort_fused(b->nblocks, b->nbins);
+    const int scans = fused ? 0 : ((int64_t)b->nbins + 1 <= kOneBlockScanMax ? 1 : 3);
+    int k = scans + (b->nblocks > 0 ? 1 : 0) + (b->ntot > 0 ? 2 : 0);
     for (const BatchStage &s : b->stages)
         k += s.grid > 0 ? 1 : 0;
     if (kernel_launches)
         *kernel_launches = k;
     if (memsets)
-        *memsets = 2;
+        *memsets = fused ? 1 : 2;
     if (device_bytes)
         *device_bytes = b->dev_bytes;
     return FB_OK;

@@ -241,24 +241,18 @@ __device__ __forceinline__ void copy_rec(const uint4 *__restrict__ rec, uint4 *_
         srec[(size_t)i * rw + w] = rec[(size_t)k * rw + w];
 }
 
-// Sorts every bin's entries by sample index: one warp per bin, in registers for
-// up to 64 entries, in shared memory up to kWarpSortMax; larger bins are listed
-// for k_sort_large.  Every sorted bin also gets its sample records copied into
-// sorted order (rw 16-byte words a record).
-__global__ void __launch_bounds__(32 * kBinSortWarps) k_sort_bins(const uint32_t *__restrict__ start, uint32_t nbins,
-                                                                  uint32_t *__restrict__ sorted,
-                                                                  uint32_t *__restrict__ large,
-                                                                  const uint4 *__restrict__ rec,
-                                                                  uint4 *__restrict__ srec, int rw)
+// Sorts one bin's entries by sample index with one warp: in registers for up
+// to 64 entries, in shared memory (`buf`, kWarpSortMax entries) up to
+// kWarpSortMax; returns false, leaving a larger bin to the whole block.  The
+// bin's sample records are copied into sorted order (rw 16-byte words a
+// record).
+__device__ __forceinline__ bool sort_one_bin(const uint32_t *__restrict__ start, int64_t b,
+                                             uint32_t *__restrict__ sorted, const uint4 *__restrict__ rec,
+                                             uint4 *__restrict__ srec, int rw, uint32_t *buf, int lane)
 {
-    __shared__ uint32_t buf[kBinSortWarps][kWarpSortMax];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t b = (int64_t)blockIdx.x * kBinSortWarps + w;
-    if (b >= nbins)
-        return;
     const uint32_t s0 = start[b], c = start[b + 1] - s0;
     if (c == 0)
-        return;
+        return true;
     if (c <= 32) {
         uint32_t x = lane < (int)c ? sorted[s0 + lane] : 0xFFFFFFFFu;
         for (int k = 2; k <= 32; k <<= 1) {
@@ -273,7 +267,7 @@ __global__ void __launch_bounds__(32 * kBinSortWarps) k_sort_bins(const uint32_t
             sorted[s0 + lane] = x;
             copy_rec(rec, srec, rw, x, s0 + lane);
         }
-        return;
+        return true;
     }
     if (c <= 64) {
         // two keys a lane (elements lane and lane + 32), bitonic network in
@@ -305,69 +299,162 @@ __global__ void __launch_bounds__(32 * kBinSortWarps) k_sort_bins(const uint32_t
             sorted[s0 + lane + 32] = x1;
             copy_rec(rec, srec, rw, x1, s0 + lane + 32);
         }
-        return;
+        return true;
     }
     if (c <= kWarpSortMax) {
         int n = 128;
         while (n < (int)c)
             n <<= 1;
-        uint32_t *s = buf[w];
         for (int i = lane; i < n; i += 32)
-            s[i] = i < (int)c ? sorted[s0 + i] : 0xFFFFFFFFu;
+            buf[i] = i < (int)c ? sorted[s0 + i] : 0xFFFFFFFFu;
         __syncwarp();
-        bitonic(s, n, lane, 32, WarpSync());
+        bitonic(buf, n, lane, 32, WarpSync());
         for (int i = lane; i < (int)c; i += 32) {
-            sorted[s0 + i] = s[i];
-            copy_rec(rec, srec, rw, s[i], s0 + i);
+            sorted[s0 + i] = buf[i];
+            copy_rec(rec, srec, rw, buf[i], s0 + i);
         }
-        return;
+        return true;
     }
-    if (lane == 0) {
-        const uint32_t slot = atomicAdd(&large[0], 1u);
-        large[1 + slot] = (uint32_t)b;
-    }
+    return false;
 }
 
-// Sorts the bins too large for one warp, one block per bin at a time, in a
-// scratch area of twice the bin size (padded to a power of two with keys that
-// sort last), and copies their records into sorted order.
-__global__ void __launch_bounds__(1024) k_sort_large(const uint32_t *__restrict__ start, uint32_t *__restrict__ sorted,
-                                                     const uint32_t *__restrict__ large,
-                                                     uint32_t *__restrict__ scratch, const uint4 *__restrict__ rec,
-                                                     uint4 *__restrict__ srec, int rw)
+// Sorts one bin too large for a warp with the whole block: in shared memory
+// (`sbuf`, cap entries) when it fits, else in a global scratch area of twice
+// the bin size (padded to a power of two with keys that sort last); copies
+// its records into sorted order.
+__device__ void sort_large_bin(const uint32_t *__restrict__ start, int64_t b, uint32_t *__restrict__ sorted,
+                               uint32_t *__restrict__ scratch, const uint4 *__restrict__ rec,
+                               uint4 *__restrict__ srec, int rw, uint32_t *sbuf, int cap)
 {
-    const uint32_t nlarge = large[0];
-    for (uint32_t q = blockIdx.x; q < nlarge; q += gridDim.x) {
-        const uint32_t b = large[1 + q];
-        const uint32_t s0 = start[b], c = start[b + 1] - s0;
-        int n = 1;
-        while (n < (int)c)
-            n <<= 1;
-        uint32_t *s = scratch + 2 * (size_t)s0;   // 2c >= n cells of this bin's own region
-        for (int i = threadIdx.x; i < n; i += blockDim.x)
-            s[i] = i < (int)c ? sorted[s0 + i] : 0xFFFFFFFFu;
-        __syncthreads();
-        bitonic(s, n, threadIdx.x, (int)blockDim.x, BlockSync());
-        for (int i = threadIdx.x; i < (int)c; i += blockDim.x) {
-            sorted[s0 + i] = s[i];
-            copy_rec(rec, srec, rw, s[i], s0 + i);
-        }
-        __syncthreads();
+    const uint32_t s0 = start[b], c = start[b + 1] - s0;
+    int n = 1;
+    while (n < (int)c)
+        n <<= 1;
+    uint32_t *sc = n <= cap ? sbuf : scratch + 2 * (size_t)s0;   // 2c >= n cells of this bin's own region
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        sc[i] = i < (int)c ? sorted[s0 + i] : 0xFFFFFFFFu;
+    __syncthreads();
+    bitonic(sc, n, threadIdx.x, (int)blockDim.x, BlockSync());
+    for (int i = threadIdx.x; i < (int)c; i += blockDim.x) {
+        sorted[s0 + i] = sc[i];
+        copy_rec(rec, srec, rw, sc[i], s0 + i);
     }
+    __syncthreads();
+}
+
+// Sorts every bin's entries by sample index, one warp per bin
+// (sort_one_bin), so each bin lists its samples in sample order whatever
+// order the count atomics produced, and copies the records into that order.
+// A block's bins too large for a warp are then sorted by the whole block, so
+// one launch covers every bin size.
+__global__ void __launch_bounds__(32 * kBinSortWarps) k_sort_bins(const uint32_t *__restrict__ start, uint32_t nbins,
+                                                                  uint32_t *__restrict__ sorted,
+                                                                  const uint4 *__restrict__ rec,
+                                                                  uint4 *__restrict__ srec, int rw,
+                                                                  uint32_t *__restrict__ scratch)
+{
+    __shared__ uint32_t buf[kBinSortWarps][kWarpSortMax];
+    __shared__ int s_big[kBinSortWarps];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t b = (int64_t)blockIdx.x * kBinSortWarps + w;
+    bool done = true;
+    if (b < nbins)
+        done = sort_one_bin(start, b, sorted, rec, srec, rw, buf[w], lane);
+    if (lane == 0)
+        s_big[w] = done ? 0 : 1;
+    __syncthreads();
+    for (int q = 0; q < kBinSortWarps; q++)
+        if (s_big[q])
+            sort_large_bin(start, (int64_t)blockIdx.x * kBinSortWarps + q, sorted, scratch, rec, srec, rw,
+                           &buf[0][0], kBinSortWarps * kWarpSortMax);
 }
 
 // ---------------------------------------------------------------------------
 // batched form: the samples of many 2D fields in one set of launches
 // ---------------------------------------------------------------------------
 
-// Bin keys and records of one block of one field's samples; keys are global
-// bins (the field's bin offset + row), records indexed by global sample.
-template <typename Real>
-__global__ void k_batch_keys(const BatchKeyField *__restrict__ fields, const uint2 *__restrict__ blocks,
-                             uint32_t skip_key, uint32_t *__restrict__ keys, SampleRec<Real> *__restrict__ rec,
-                             uint32_t *__restrict__ counts, uint32_t *__restrict__ rank,
-                             FieldHeader *__restrict__ hdrs)
+// Exclusive scan of counts[0, n) into bin_start by one block of 256 threads
+// (the last block of the key pass), which also clears the counts for the
+// next run.  Tiles of 1024 entries, one 16-byte load a thread, the next
+// tile's load issued before the current tile is scanned.  The counts were
+// built by device-scope atomics: read from L2.  counts must have readable
+// (ignored) entries up to n rounded up to 4.
+__device__ void last_block_scan(uint32_t *__restrict__ counts, uint32_t *__restrict__ bin_start, int64_t n)
 {
+    __shared__ uint32_t s_w[8];
+    __shared__ uint32_t s_tot;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const int64_t ntile = (n + 1023) / 1024;
+    auto load = [&](int64_t tile) -> uint4 {
+        const int64_t base = tile * 1024 + 4 * t;
+        return base < n ? __ldcg(reinterpret_cast<const uint4 *>(counts + base)) : make_uint4(0u, 0u, 0u, 0u);
+    };
+    uint32_t carry = 0;
+    uint4 cur = load(0);
+    for (int64_t tile = 0; tile < ntile; tile++) {
+        const uint4 nxt = tile + 1 < ntile ? load(tile + 1) : make_uint4(0u, 0u, 0u, 0u);
+        const int64_t base = tile * 1024 + 4 * t;
+        uint32_t x[4] = {cur.x, cur.y, cur.z, cur.w};
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (base + u >= n)
+                x[u] = 0u;
+        const uint32_t sum = x[0] + x[1] + x[2] + x[3];
+        uint32_t inc = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o)
+                inc += y;
+        }
+        if (lane == 31)
+            s_w[w] = inc;
+        __syncthreads();
+        if (w == 0) {
+            const uint32_t v = lane < 8 ? s_w[lane] : 0u;
+            uint32_t vi = v;
+#pragma unroll
+            for (int o = 1; o < 8; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, vi, o);
+                if (lane >= o)
+                    vi += y;
+            }
+            if (lane < 8)
+                s_w[lane] = vi - v;
+            if (lane == 7)
+                s_tot = vi;
+        }
+        __syncthreads();
+        uint32_t run = carry + s_w[w] + inc - sum;
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            if (base + u < n) {
+                bin_start[base + u] = run;
+                counts[base + u] = 0u;
+            }
+            run += x[u];
+        }
+        carry += s_tot;
+        __syncthreads();   // s_w / s_tot are rewritten by the next tile
+        cur = nxt;
+    }
+}
+
+// Bin keys and records of one block of one field's samples (256 threads, two
+// samples each, both loaded before either is worked on); keys are global
+// bins (the field's bin offset + row), records indexed by global sample.
+// FUSED: the last block to finish (a ticket counter) scans the bin counts
+// into bin_start and clears the counts and the ticket for the next run, so
+// that no separate scan launch or memset is needed.
+template <typename Real, bool FUSED>
+__global__ void __launch_bounds__(256) k_batch_keys(const BatchKeyField *__restrict__ fields,
+                                                    const uint2 *__restrict__ blocks, uint32_t skip_key,
+                                                    uint32_t *__restrict__ keys, SampleRec<Real> *__restrict__ rec,
+                                                    uint32_t *__restrict__ counts, uint32_t *__restrict__ rank,
+                                                    FieldHeader *__restrict__ hdrs, uint32_t *ticket,
+                                                    uint32_t *__restrict__ bin_start, int64_t nscan)
+{
+    static_assert(kBatchKeysPerBlock == 512, "two samples per thread of 256");
     // Float64 instructions are few per SM on this part, so the loop keeps
     // them to the cell coordinates: the NaN test works on the bits, the
     // upper bound of the skip rule on the truncated cell index (trunc = floor
@@ -380,22 +467,35 @@ __global__ void k_batch_keys(const BatchKeyField *__restrict__ fields, const uin
     unsigned long long kmin = ~0ull, kmax = 0ull;
     int nan = 0;
     const int64_t end = min(f.npts, (int64_t)bt.y + kBatchKeysPerBlock);
-    for (int64_t k = (int64_t)bt.y + threadIdx.x; k < end; k += blockDim.x) {
-        const double v = f.val[k];
-        const unsigned long long vb = (unsigned long long)__double_as_longlong(v);
+    int64_t ks[2];
+    double v[2], px[2], py[2];
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+        ks[u] = (int64_t)bt.y + threadIdx.x + u * 256;
+        if (ks[u] < end) {
+            v[u] = f.val[ks[u]];
+            px[u] = f.pts[2 * ks[u]];
+            py[u] = f.pts[2 * ks[u] + 1];
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+        if (ks[u] >= end)
+            continue;
+        const int64_t k = ks[u];
+        const unsigned long long vb = (unsigned long long)__double_as_longlong(v[u]);
         if ((vb & 0x7fffffffffffffffull) > 0x7ff0000000000000ull) {
             nan = 1;
         } else {
-            unsigned long long o = dbl_to_ordered(v);
+            unsigned long long o = dbl_to_ordered(v[u]);
             kmin = o < kmin ? o : kmin;
             kmax = o > kmax ? o : kmax;
         }
-        const double *p = f.pts + 2 * k;
         int xi, yi;
         Real xw, yw;
         bool skip;
         if (EXACT) {
-            const double xc = (p[0] - f.x0[0]) / f.step[0], yc = (p[1] - f.x0[1]) / f.step[1];
+            const double xc = (px[u] - f.x0[0]) / f.step[0], yc = (py[u] - f.x0[1]) / f.step[1];
             xi = __double2int_rz(xc);
             yi = __double2int_rz(yc);
             skip = !(xc >= 0.0) || !(yc >= 0.0);
@@ -403,8 +503,8 @@ __global__ void k_batch_keys(const BatchKeyField *__restrict__ fields, const uin
             yw = (Real)(yc - (double)yi);
         } else {
             float xf, yf;
-            skip = !split_cell((p[0] - f.x0[0]) * f.inv_step[0], xi, xf) ||
-                   !split_cell((p[1] - f.x0[1]) * f.inv_step[1], yi, yf);
+            skip = !split_cell((px[u] - f.x0[0]) * f.inv_step[0], xi, xf) ||
+                   !split_cell((py[u] - f.x0[1]) * f.inv_step[1], yi, yf);
             xw = (Real)xf;
             yw = (Real)yf;
         }
@@ -420,7 +520,7 @@ __global__ void k_batch_keys(const BatchKeyField *__restrict__ fields, const uin
             r.yw = yw;
             key = f.bin_offset + (uint32_t)yi;
         }
-        r.val = v;
+        r.val = v[u];
         const int64_t gk = f.sample_offset + k;
         rec[gk] = r;
         keys[gk] = key;
@@ -428,6 +528,20 @@ __global__ void k_batch_keys(const BatchKeyField *__restrict__ fields, const uin
             rank[gk] = atomicAdd(&counts[key], 1u);   // the sample's slot in its bin (any order)
     }
     range_to_header(kmin, kmax, nan, hdrs + bt.x);
+    if constexpr (FUSED) {
+        __shared__ bool s_last;
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0)
+            s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+        __syncthreads();
+        if (!s_last)
+            return;
+        __threadfence();
+        last_block_scan(counts, bin_start, nscan);
+        if (threadIdx.x == 0)
+            *ticket = 0u;
+    }
 }
 
 // Device-wide exclusive scan in three steps: sums of 4096-entry tiles, an
@@ -504,7 +618,8 @@ __global__ void __launch_bounds__(1024) k_tile_scan(const uint32_t *__restrict__
 }
 
 
-// Scratch layout: counts[nbins + 2] | cursor[nbins + 2] | large[nbins + 2] |
+// Scratch layout: counts[nbins + 2] | cursor[nbins + 2] (cursor[0]: the
+// batched key pass's ticket) | large[nbins + 2] (spare) |
 // keys[N] | sorted[N] | big-bin scratch[2N] (uint32; its first N entries hold
 // the samples' slots in their bins until the scatter), then the sample records
 // by sample index, the records in sorted order, and (batched form) the
@@ -588,32 +703,47 @@ cudaError_t batch_sort(int precision, const BatchKeyField *d_fields, const uint2
                        uint32_t *bin_start, const uint32_t **sorted_idx, const void **recs, cudaStream_t st)
 {
     const SortLayout l = sort_layout(scratch, ntot, nbins, precision);
+    const int64_t n = (int64_t)nbins + 1;
+    // one launch for keys and bin starts when the bin starts fit one block's
+    // scan; the counts then stay zero between runs (the scanning block
+    // clears them; the plan clears them once at creation)
+    const bool fused = nblocks > 0 && n <= kOneBlockScanMax;
     cudaError_t e = cudaMemsetAsync(hdrs, 0, sizeof(FieldHeader) * (size_t)nfields, st);
-    if (e == cudaSuccess)
+    if (e == cudaSuccess && !fused)
         e = cudaMemsetAsync(l.counts, 0, sizeof(uint32_t) * 3 * ((size_t)nbins + 2), st);
     if (e != cudaSuccess)
         return e;
     *sorted_idx = l.sorted;
     *recs = l.srec;
+    uint32_t *ticket = l.cursor;
+#define FBG_BK(R, F)                                                                                               \
+    k_batch_keys<R, F><<<nblocks, 256, 0, st>>>(d_fields, d_blocks, nbins, l.keys,                                 \
+                                                reinterpret_cast<SampleRec<R> *>(l.rec), l.counts, l.big, hdrs,    \
+                                                ticket, bin_start, n)
     if (nblocks > 0) {
-        if (precision == 0)
-            k_batch_keys<double><<<nblocks, 256, 0, st>>>(d_fields, d_blocks, nbins, l.keys,
-                                                           reinterpret_cast<SampleRec<double> *>(l.rec), l.counts,
-                                                           l.big, hdrs);
-        else
-            k_batch_keys<float><<<nblocks, 256, 0, st>>>(d_fields, d_blocks, nbins, l.keys,
-                                                          reinterpret_cast<SampleRec<float> *>(l.rec), l.counts,
-                                                          l.big, hdrs);
+        if (precision == 0) {
+            if (fused)
+                FBG_BK(double, true);
+            else
+                FBG_BK(double, false);
+        } else {
+            if (fused)
+                FBG_BK(float, true);
+            else
+                FBG_BK(float, false);
+        }
     }
-    const int64_t n = (int64_t)nbins + 1;
-    if (n <= kOneBlockScanMax) {
-        k_scan_exclusive<<<1, 1024, 0, st>>>(l.counts, bin_start, n);
-    } else {
-        const unsigned tiles = (unsigned)((n + 4095) / 4096);
-        k_tile_sums<<<tiles, 1024, 0, st>>>(l.counts, n, l.tsum);
-        uint32_t *toff = l.tsum + tiles;
-        k_scan_exclusive<<<1, 1024, 0, st>>>(l.tsum, toff, (int64_t)tiles);
-        k_tile_scan<<<tiles, 1024, 0, st>>>(l.counts, n, toff, bin_start);
+#undef FBG_BK
+    if (!fused) {
+        if (n <= kOneBlockScanMax) {
+            k_scan_exclusive<<<1, 1024, 0, st>>>(l.counts, bin_start, n);
+        } else {
+            const unsigned tiles = (unsigned)((n + 4095) / 4096);
+            k_tile_sums<<<tiles, 1024, 0, st>>>(l.counts, n, l.tsum);
+            uint32_t *toff = l.tsum + tiles;
+            k_scan_exclusive<<<1, 1024, 0, st>>>(l.tsum, toff, (int64_t)tiles);
+            k_tile_scan<<<tiles, 1024, 0, st>>>(l.counts, n, toff, bin_start);
+        }
     }
     if (ntot > 0) {
         int blocks = (int)std::min<int64_t>((ntot + 255) / 256, (int64_t)1 << 22);
@@ -622,11 +752,12 @@ cudaError_t batch_sort(int precision, const BatchKeyField *d_fields, const uint2
         const uint4 *rec4 = reinterpret_cast<const uint4 *>(l.rec);
         uint4 *srec4 = reinterpret_cast<uint4 *>(l.srec);
         k_sort_bins<<<(unsigned)((nbins + kBinSortWarps - 1) / kBinSortWarps), 32 * kBinSortWarps, 0, st>>>(
-            bin_start, nbins, l.sorted, l.large, rec4, srec4, rw);
-        k_sort_large<<<64, 1024, 0, st>>>(bin_start, l.sorted, l.large, l.big, rec4, srec4, rw);
+            bin_start, nbins, l.sorted, rec4, srec4, rw, l.big);
     }
     return cudaGetLastError();
 }
+
+bool batch_sort_fused(uint32_t nblocks, uint32_t nbins) { return nblocks > 0 && (int64_t)nbins + 1 <= kOneBlockScanMax; }
 
 cudaError_t sort_samples(int precision, const double *pts, const double *val, int64_t npts, const Geometry &g,
                          int bin_w, uint32_t nbins, FieldHeader *hdr, uint32_t *scratch, uint32_t *bin_start,
@@ -670,8 +801,7 @@ cudaError_t sort_samples(int precision, const double *pts, const double *val, in
         const uint4 *rec4 = reinterpret_cast<const uint4 *>(l.rec);
         uint4 *srec4 = reinterpret_cast<uint4 *>(l.srec);
         k_sort_bins<<<(unsigned)((nbins + kBinSortWarps - 1) / kBinSortWarps), 32 * kBinSortWarps, 0, st>>>(
-            bin_start, nbins, l.sorted, l.large, rec4, srec4, rw);
-        k_sort_large<<<64, 1024, 0, st>>>(bin_start, l.sorted, l.large, l.big, rec4, srec4, rw);
+            bin_start, nbins, l.sorted, rec4, srec4, rw, l.big);
     }
     return cudaGetLastError();
 }

@@ -143,7 +143,9 @@ def test_batch_headline_shape_knobs_and_tuning():
         for (p, v), (ref_out, ref_q, wg, thr), o in zip(host, refs, outs):
             check_fp32c(o, ref_q, wg, thr)
         launches, memsets, nbytes = plan.info
-        assert launches == 7 and memsets == 2 and nbytes > 0
+        # keys with the bin-start scan, scatter, bin sort, x axis, y axis;
+        # one memset (field headers)
+        assert launches == 5 and memsets == 1 and nbytes > 0
         plan.close()
     assert len(seen) >= 3
 
