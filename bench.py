@@ -545,7 +545,40 @@ def main():
     e1_.synchronize()
     link_gbs = 3 * B * W * H * 4 / (e0_.elapsed_time(e1_) * 1e-3) / 1e9
     link_bound = W * H * B / (B * W * H * 4 / (link_gbs * 1e9)) / 1e6
+    # host -> device over the same link (the samples' direction)
+    with torch.cuda.stream(streams[0]):
+        e0_, e1_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0_.record()
+        for _ in range(3):
+            dev_res.copy_(pin_res, non_blocking=True)
+        e1_.record()
+    e1_.synchronize()
+    link_h2d_gbs = 3 * B * W * H * 4 / (e0_.elapsed_time(e1_) * 1e-3) / 1e9
     del dev_res, pin_res
+
+    # ---- e2e_dropin: the call a reference user makes -----------------------
+    # interpolation.barnes(pts, val, ...) on one headline field with numpy
+    # arrays in and a float32 numpy array out (the C ABI's host-buffer entry
+    # underneath), synchronous like the reference's.  Bound: the field's
+    # samples in and its result out over the host link, at the rates just
+    # measured.
+    from fastbarnes_gb300 import interpolation as FI
+    pts0, val0 = host[0]
+
+    def dropin():
+        return FI.barnes(pts0, val0, SIGMA, X0, STEP, (W, H), num_iter=NITER, max_dist=MAX_DIST,
+                         precision=args.precision)
+
+    for _ in range(3):
+        r0 = dropin()
+    k_drop = max(5, args.steps // 2)
+    t0 = time.perf_counter()
+    for _ in range(k_drop):
+        r0 = dropin()
+    drop_s = (time.perf_counter() - t0) / k_drop
+    drop_value = W * H / drop_s / 1e6
+    drop_bound = W * H / (NPTS * 24 / (link_h2d_gbs * 1e9) + W * H * 4 / (link_gbs * 1e9)) / 1e6
+    drop_ok = bool(np.array_equal(r0, plan.outs[0].cpu().numpy(), equal_nan=True))
     for p in h_pts + h_val + h_out[0] + h_out[1]:
         L.fb_host_free(p)
     plan.close()
@@ -623,6 +656,12 @@ def main():
                         "windows": {"steps_each": k_e2e, "values": e2e_runs, "reported": "median"},
                         "entry": "fb_batch_enqueue_host (pinned host buffers; two plans on two streams, "
                                  "each step's copies overlap the next step's interpolation)"},
+                "e2e_dropin": {"value": drop_value, "unit": "Mgridpts/s", "ms_per_field": drop_s * 1e3,
+                               "h2d_bytes_per_field": NPTS * 24, "d2h_bytes_per_field": W * H * 4,
+                               "link_h2d_gbs": link_h2d_gbs, "link_bound_value": drop_bound,
+                               "frac_of_link_bound": drop_value / drop_bound, "matches_batch_result": drop_ok,
+                               "entry": "fastbarnes_gb300.interpolation.barnes(numpy pts, numpy val, ...) -> "
+                                        "float32 numpy, one 4096x2048 field per call (fb_interpolate_host)"},
                 "cpu_baseline": cpu, "clocks": clk.summary(),
                 "plan": {"kernel_launches_per_step": launches_per_step, "memsets_per_step": memsets_per_step,
                          "device_bytes": plan_bytes}}

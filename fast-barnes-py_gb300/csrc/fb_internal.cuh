@@ -101,6 +101,30 @@ __device__ __forceinline__ bool split_cell(double t, int &ci, float &cw)
     return true;
 }
 
+// Float32-form cell coordinate of a sample with the reference's skip rule
+// kept exact at the grid's upper edge: q = p - x0 (the reference's
+// difference), t = q * inv (1 / step, a product instead of the reference's
+// division).  A sample whose cell lands in the last valid cell or beyond
+// (index >= size - 2, about one sample in size) is redone with the
+// reference's division, so that xc >= size - 1 skips it exactly when the
+// reference does (interpolation.py:249-252).  Returns false for a skipped
+// sample.
+__device__ __forceinline__ bool split_cell_edge(double q, double step, double inv, int64_t size, int &ci, float &cw)
+{
+    if (!split_cell(q * inv, ci, cw))
+        return false;
+    if ((int64_t)ci >= size - 2) {
+        const double xc = q / step;
+        if (!(xc >= 0.0))
+            return false;
+        ci = __double2int_rz(xc);
+        if ((int64_t)ci >= size - 1)
+            return false;
+        cw = (float)(xc - (double)ci);
+    }
+    return true;
+}
+
 // Geometry and parameters of one interpolation, shared by all kernels.
 struct Geometry {
     int dim;

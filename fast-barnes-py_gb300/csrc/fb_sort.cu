@@ -99,7 +99,7 @@ __global__ void k_bin_keys(const double *__restrict__ pts, const double *__restr
                 cw[m] = (Real)(c[m] - (double)ci[m]);
             } else {
                 float f;
-                skip = skip || !split_cell((p[m] - g.x0[m]) * s_inv[m], ci[m], f);
+                skip = skip || !split_cell_edge(p[m] - g.x0[m], g.step[m], s_inv[m], g.size[m], ci[m], f);
                 cw[m] = (Real)f;
             }
             skip = skip || (int64_t)ci[m] >= g.size[m] - 1;
@@ -503,8 +503,8 @@ __global__ void __launch_bounds__(256) k_batch_keys(const BatchKeyField *__restr
             yw = (Real)(yc - (double)yi);
         } else {
             float xf, yf;
-            skip = !split_cell((px[u] - f.x0[0]) * f.inv_step[0], xi, xf) ||
-                   !split_cell((py[u] - f.x0[1]) * f.inv_step[1], yi, yf);
+            skip = !split_cell_edge(px[u] - f.x0[0], f.step[0], f.inv_step[0], f.size[0], xi, xf) ||
+                   !split_cell_edge(py[u] - f.x0[1], f.step[1], f.inv_step[1], f.size[1], yi, yf);
             xw = (Real)xf;
             yw = (Real)yf;
         }

@@ -158,6 +158,46 @@ def workspace(nbytes, device):
     return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
 
 
+class _PinnedPool:
+    """Page-locked host buffers (fb_host_alloc) for numpy results: a result
+    array wraps one buffer, so the device-to-host copy is one DMA straight
+    into it; when the array is freed the buffer returns here (up to
+    `keep` free buffers are cached, the rest released)."""
+
+    def __init__(self, keep=4):
+        self.keep = keep
+        self.free = {}
+        self.lock = threading.Lock()
+
+    def empty(self, shape, dtype):
+        import weakref
+        import numpy as np
+        dtype = np.dtype(dtype)
+        nbytes = max(int(np.prod(shape)) * dtype.itemsize, 16)
+        with self.lock:
+            bucket = self.free.get(nbytes)
+            ptr = bucket.pop() if bucket else None
+        if ptr is None:
+            ptr = lib().fb_host_alloc(nbytes)
+            if not ptr:
+                raise FastBarnesError(f"fb_host_alloc({nbytes}) failed")
+        buf = (ctypes.c_char * nbytes).from_address(ptr)
+        arr = np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+        weakref.finalize(buf, self._put, ptr, nbytes)
+        return arr
+
+    def _put(self, ptr, nbytes):
+        with self.lock:
+            bucket = self.free.setdefault(nbytes, [])
+            if sum(len(b) for b in self.free.values()) < self.keep:
+                bucket.append(ptr)
+                return
+        lib().fb_host_free(ptr)
+
+
+pinned = _PinnedPool()
+
+
 def stream_ptr(torch, device):
     return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
 

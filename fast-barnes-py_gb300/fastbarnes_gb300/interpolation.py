@@ -158,10 +158,38 @@ def _precision_code(precision):
 # device execution
 # ---------------------------------------------------------------------------
 
+def _run_grid_host(method_code, prec, dim, pts, val, sigma, x0, step, size, num_iter, max_dist_weight, out_dtype):
+    """numpy in, numpy out: one call of the C ABI's host-buffer entry
+    (fb_interpolate_host: copies in, the interpolation and the copy out on
+    torch's current stream, with the library's device buffer; no torch
+    tensors), which also checks the device status word.  The result array
+    wraps a page-locked buffer of the library's pool, so the result comes
+    back as one DMA transfer."""
+    torch = _lib.torch_cuda()
+    npts = int(val.shape[0])
+    hp = np.ascontiguousarray(pts, dtype=np.float64).reshape(npts, dim)
+    hv = np.ascontiguousarray(val, dtype=np.float64)
+    out_f64 = 1 if np.dtype(out_dtype) == np.float64 else 0
+    out = _lib.pinned.empty(tuple(int(s) for s in size[::-1]), np.float64 if out_f64 else np.float32)
+    L = _lib.lib()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    with torch.cuda.device(dev):
+        rc = L.fb_interpolate_host(method_code, prec, dim, hp.ctypes.data, hv.ctypes.data, npts,
+                                   _lib.dvec([float(s) for s in sigma]), _lib.dvec([float(s) for s in x0]),
+                                   _lib.dvec([float(s) for s in step]), _lib.dvec([int(s) for s in size], ctypes.c_int64),
+                                   int(num_iter), float(max_dist_weight), out.ctypes.data, out_f64,
+                                   _lib.stream_ptr(torch, dev))
+        _lib.check(rc, "fb_interpolate_host")
+    return out
+
+
 def _run_grid(method_code, prec, dim, pts, val, sigma, x0, step, size, num_iter, max_dist_weight, out_dtype,
               tensor_in):
     """Runs fb_interpolate on the current CUDA device; returns numpy or torch."""
     torch = _lib.torch_cuda()
+    if not tensor_in:
+        return _run_grid_host(method_code, prec, dim, pts, val, sigma, x0, step, size, num_iter, max_dist_weight,
+                              out_dtype)
     if tensor_in:
         dev = pts.device if _is_tensor(pts) and pts.is_cuda else torch.device("cuda", torch.cuda.current_device())
     else:

@@ -89,9 +89,12 @@ int fb_interpolate(int method, int precision, int dim, const double *d_pts, cons
 
 /* Same computation from host buffers: copies pts / val to the device, runs
  * fb_interpolate on `stream` with a library-owned device buffer (grown on
- * demand, released by fb_release), copies the result into host `out` and
- * synchronizes the stream.  Pinned host memory (fb_host_alloc) makes the
- * copies asynchronous DMA transfers. */
+ * demand, released by fb_release), copies the result into host `out`,
+ * synchronizes the stream and checks the device status word (FB_ERR_DEVICE).
+ * Pinned host memory (fb_host_alloc) makes the copies asynchronous DMA
+ * transfers.  The library's device buffer is one per process: calls from
+ * several host threads are serialized (one at a time, copies and
+ * synchronization included). */
 int fb_interpolate_host(int method, int precision, int dim, const double *pts, const double *val,
                         int64_t n_pts, const double *sigma, const double *x0, const double *step,
                         const int64_t *size, int num_iter, double max_dist_weight, void *out, int out_f64,
