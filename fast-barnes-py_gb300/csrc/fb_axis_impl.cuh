@@ -693,8 +693,12 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
     const int T = a.T;
     // sliding passes need the chunks of both grids that touch [0, E)
     const int nact = MODE == 1 ? nch : (E + T + 1 + K - 1) / K;
-    const bool active = li < nl && j < nact;
+    bool active = li < nl && j < nact;
     const int q = (2 * T + 1) / K, r = (2 * T + 1) - q * K;
+    // bounds-check build: every pass window of this thread inside the buffers
+    if (kBoundsCheck && active)
+        active = bounds_ok(pass_windows_in(j, K, T, E, HP, P, PP, PF, q, MODE == 1),
+                           fp.hdr ? &fp.hdr->error : nullptr);
     // The field's offset and the float32 form's scalar parameters are
     // computed once per CTA: float64 instructions (including conversions to
     // float32) are scarce, and every thread needs them.
@@ -757,9 +761,11 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
             if (li < nl) {
                 for (int q = j; q < kStage; q += CP) {
                     const uint32_t pos = base + q;
-                    if (pos < total)
-                        my_stage[q] = make_stage<SPLAT_DIM, Real>(recs[range_at(rg, pos)], line0 + li,
-                                                                  g, offset);
+                    if (pos < total) {
+                        const uint32_t idx = range_at(rg, pos);
+                        if (bounds_ok(idx < (uint64_t)sv.npts, &fp.hdr->error))
+                            my_stage[q] = make_stage<SPLAT_DIM, Real>(recs[idx], line0 + li, g, offset);
+                    }
                 }
             }
             __syncthreads();

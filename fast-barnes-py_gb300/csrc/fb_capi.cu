@@ -46,7 +46,10 @@ static int device_fail(uint32_t bits, const char *where)
                 (bits & FB_DEVICE_BOUNDS) ? " (an out-of-range index was skipped: bounds-check build)" : "");
 }
 
-extern "C" const char *fb_version(void) { return "fastbarnes_gb300 0.1 (sm_103a)"; }
+extern "C" const char *fb_version(void)
+{
+    return kBoundsCheck ? "fastbarnes_gb300 0.1 (sm_103a, bounds-check build)" : "fastbarnes_gb300 0.1 (sm_103a)";
+}
 extern "C" const char *fb_last_error(void) { return g_err; }
 
 extern "C" int fb_tune(const char *name, int value)

@@ -246,7 +246,12 @@ __global__ void __maxnreg__((ColsRegs<Real, K, MODE>::value))
         C *cells = reinterpret_cast<C *>(base + (size_t)s * p.stage_bytes) + (size_t)HP * G;
         C *ln = cells + li;
         const uint32_t xb = (t % p.tiles_per_field) % p.xblocks;
-        const bool active = j < nact && (int64_t)xb * G + li < p.width;
+        bool active = j < nact && (int64_t)xb * G + li < p.width;
+        // bounds-check build: every pass window of this thread inside the stage
+        if (kBoundsCheck && active)
+            active = bounds_ok(pass_windows_in(j, K, T, E, HP, p.line_pitch, PP, PF, q, MODE == 1) &&
+                                   HP + p.nboxes * p.box_rows <= p.line_pitch,
+                               p.status);
         C o_[K];
         int a_last = 0;   // first cell of the chunk the last pass produced
 

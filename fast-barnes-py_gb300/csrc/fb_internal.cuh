@@ -259,6 +259,47 @@ struct MixedField {
 constexpr uint32_t FB_DEVICE_TIMEOUT = 1u;   // a pipeline wait ran out
 constexpr uint32_t FB_DEVICE_BOUNDS = 2u;    // bounds-check build: an out-of-range index was skipped
 
+// Bounds-check build (compiled with -DFB_BOUNDS_CHECK): kernels check their
+// shared- and global-memory index ranges before using them; an index out of
+// range is not used and FB_DEVICE_BOUNDS is recorded in the status word.
+// The checks compile away otherwise.
+#ifdef FB_BOUNDS_CHECK
+constexpr bool kBoundsCheck = true;
+#else
+constexpr bool kBoundsCheck = false;
+#endif
+
+__device__ __forceinline__ bool bounds_ok(bool ok, const void *status_word)
+{
+    if (!kBoundsCheck)
+        return true;
+    if (!ok && status_word)
+        atomicOr(reinterpret_cast<unsigned int *>(const_cast<void *>(status_word)), FB_DEVICE_BOUNDS);
+    return ok;
+}
+
+// Every line-buffer and partial-sum index the passes of one thread use
+// (chunk j, chunk length K, half width T, line extent E; HP zero cells
+// before cell 0 and P cells per line slot; PF / PP the same for the partial
+// sums; q = (2T + 1) / K): the sliding passes read [jK - 2T - 2, ...) (left)
+// and [min(jK, E - 1) + T, ...) (right) and write their chunks at jK - T - 1
+// and jK; the direct sums read [jK - T - 1, jK + K + T + 1).  True when all
+// of them lie inside the buffers.
+__device__ __forceinline__ bool pass_windows_in(int j, int K, int T, int E, int HP, int P, int PP, int PF, int q,
+                                                bool direct)
+{
+    const int lo = -HP, hi = P - HP;
+    const int b = j * K;
+    if (direct)
+        return b - T - 1 >= lo && b + K + T + 1 <= hi;
+    const int left_read = max(b - 2 * T - 2, lo);
+    const int right_read = min(b, E - 1) + T;
+    bool ok = left_read + K + 1 <= hi && b - T - 1 >= lo && b + K <= hi && right_read >= lo &&
+              right_read + 1 + K <= hi;
+    ok = ok && j - q - 1 >= -PF && j + q + 1 < PP - PF;
+    return ok;
+}
+
 // Launch description of the pipelined columns kernel (fb_cols.cuh),
 // host-computed.
 struct ColsPipe {

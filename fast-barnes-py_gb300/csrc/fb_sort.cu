@@ -190,13 +190,17 @@ __global__ void __launch_bounds__(1024) k_scan_exclusive(const uint32_t *__restr
 // order inside a bin is fixed later.
 __global__ void k_bin_scatter(const uint32_t *__restrict__ keys, int64_t npts, uint32_t nbins,
                               const uint32_t *__restrict__ start, const uint32_t *__restrict__ rank,
-                              uint32_t *__restrict__ sorted)
+                              uint32_t *__restrict__ sorted, uint32_t *status)
 {
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < npts;
          k += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t key = keys[k];
-        if (key < nbins)
-            sorted[start[key] + rank[k]] = (uint32_t)k;
+        if (key < nbins) {
+            const uint32_t pos = start[key] + rank[k];
+            // bounds-check build: inside the key's bin
+            if (bounds_ok(!kBoundsCheck || pos < start[key + 1], status))
+                sorted[pos] = (uint32_t)k;
+        }
     }
 }
 
@@ -351,14 +355,15 @@ __global__ void __launch_bounds__(32 * kBinSortWarps) k_sort_bins(const uint32_t
                                                                   uint32_t *__restrict__ sorted,
                                                                   const uint4 *__restrict__ rec,
                                                                   uint4 *__restrict__ srec, int rw,
-                                                                  uint32_t *__restrict__ scratch)
+                                                                  uint32_t *__restrict__ scratch, uint32_t *status)
 {
     __shared__ uint32_t buf[kBinSortWarps][kWarpSortMax];
     __shared__ int s_big[kBinSortWarps];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t b = (int64_t)blockIdx.x * kBinSortWarps + w;
     bool done = true;
-    if (b < nbins)
+    // bounds-check build: the bin inside the sorted arrays
+    if (b < nbins && bounds_ok(!kBoundsCheck || (start[b] <= start[b + 1] && start[b + 1] <= start[nbins]), status))
         done = sort_one_bin(start, b, sorted, rec, srec, rw, buf[w], lane);
     if (lane == 0)
         s_big[w] = done ? 0 : 1;
@@ -747,12 +752,13 @@ cudaError_t batch_sort(int precision, const BatchKeyField *d_fields, const uint2
     }
     if (ntot > 0) {
         int blocks = (int)std::min<int64_t>((ntot + 255) / 256, (int64_t)1 << 22);
-        k_bin_scatter<<<blocks, 256, 0, st>>>(l.keys, ntot, nbins, bin_start, l.big, l.sorted);
+        k_bin_scatter<<<blocks, 256, 0, st>>>(l.keys, ntot, nbins, bin_start, l.big, l.sorted,
+                                              reinterpret_cast<uint32_t *>(&hdrs->error));
         const int rw = (int)(rec_bytes(precision) / 16);
         const uint4 *rec4 = reinterpret_cast<const uint4 *>(l.rec);
         uint4 *srec4 = reinterpret_cast<uint4 *>(l.srec);
         k_sort_bins<<<(unsigned)((nbins + kBinSortWarps - 1) / kBinSortWarps), 32 * kBinSortWarps, 0, st>>>(
-            bin_start, nbins, l.sorted, rec4, srec4, rw, l.big);
+            bin_start, nbins, l.sorted, rec4, srec4, rw, l.big, reinterpret_cast<uint32_t *>(&hdrs->error));
     }
     return cudaGetLastError();
 }
@@ -796,12 +802,13 @@ cudaError_t sort_samples(int precision, const double *pts, const double *val, in
     k_scan_exclusive<<<1, 1024, 0, st>>>(l.counts, bin_start, (int64_t)nbins + 1);
     if (npts > 0) {
         int blocks = (int)std::min<int64_t>((npts + 255) / 256, (int64_t)1 << 22);
-        k_bin_scatter<<<blocks, 256, 0, st>>>(l.keys, npts, nbins, bin_start, l.big, l.sorted);
+        k_bin_scatter<<<blocks, 256, 0, st>>>(l.keys, npts, nbins, bin_start, l.big, l.sorted,
+                                              reinterpret_cast<uint32_t *>(&hdr->error));
         const int rw = (int)(rec_bytes(precision) / 16);
         const uint4 *rec4 = reinterpret_cast<const uint4 *>(l.rec);
         uint4 *srec4 = reinterpret_cast<uint4 *>(l.srec);
         k_sort_bins<<<(unsigned)((nbins + kBinSortWarps - 1) / kBinSortWarps), 32 * kBinSortWarps, 0, st>>>(
-            bin_start, nbins, l.sorted, rec4, srec4, rw, l.big);
+            bin_start, nbins, l.sorted, rec4, srec4, rw, l.big, reinterpret_cast<uint32_t *>(&hdr->error));
     }
     return cudaGetLastError();
 }

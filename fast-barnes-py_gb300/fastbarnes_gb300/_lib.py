@@ -10,7 +10,9 @@ import os
 import threading
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libfastbarnes_gb300.so")
+# FASTBARNES_GB300_LIB selects another build of the library (for instance the
+# bounds-check variant, libfastbarnes_gb300_checked.so)
+LIB_PATH = os.environ.get("FASTBARNES_GB300_LIB") or os.path.join(HERE, "libfastbarnes_gb300.so")
 
 FB_OK = 0
 FB_ERR_ARG, FB_ERR_KERNEL_SIZE, FB_ERR_WORKSPACE, FB_ERR_CUDA, FB_ERR_UNSUPPORTED, FB_ERR_DEVICE = 1, 2, 3, 4, 5, 6
