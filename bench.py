@@ -354,7 +354,9 @@ def main():
     alg = {0: B * NPTS * (24 + 4 * 6),
            1: B * (NPTS * 28 + W * H * 2 * sz),
            2: B * (W * H * 2 * sz + W * H * 4)}
-    names = {0: "sample sort", 1: "k_axis_batch x (splat fused)", 2: "k_axis_batch y (quotient fused)"}
+    alg[3] = alg[1] + alg[2]
+    names = {0: "sample sort", 1: "k_axis_batch x (splat fused)", 2: "k_axis_batch y (quotient fused)",
+             3: "k_axis_batch x and y, interleaved per field on two streams"}
     # DRAM bytes (read + write) of each axis launch per field, from the ncu
     # capture of the same kernels on 2 fields of this shape (the full-set
     # capture of the profile summaries), scaled to B fields: the traffic
@@ -626,12 +628,14 @@ def main():
                                                                  "knobs": {"chunk": knobs[0],
                                                                            "rows_threads": knobs[1],
                                                                            "mixed": knobs[2],
-                                                                           "cols_pipe": knobs[3]}},
+                                                                           "cols_pipe": knobs[3],
+                                                                           "interleave": knobs[4]}},
                 "gpu_launches": launches_per_step * args.steps,
                 "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
                              "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                              "traffic": (traffic_per_field[dom] * B
-                                         if prec == _lib.FB_FP32C and (W, H) == (4096, 2048) else None),
+                                         if prec == _lib.FB_FP32C and (W, H) == (4096, 2048)
+                                         and dom in traffic_per_field else None),
                              "traffic_source": "ncu capture of 2 fields, scaled to the batch",
                              "algorithmic_bytes_per_launch": alg[dom],
                              "launch_ms": stage_ms[dom],

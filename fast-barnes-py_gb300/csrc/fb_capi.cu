@@ -1053,6 +1053,12 @@ struct fb_batch {
     cudaStream_t cap = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    // interleaved runs: the second stream and the events ordering field f's
+    // y launch after its x launch
+    bool interleave = false;
+    cudaStream_t side = nullptr;
+    std::vector<cudaEvent_t> ev_field;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // host-buffer runs: result copies spread over several streams (copy
     // engines), made at the first fb_batch_run_host
     static constexpr int kCopyStreams = 4;
@@ -1070,6 +1076,17 @@ void batch_free(fb_batch *b)
         cudaGraphDestroy(b->graph);
     if (b->cap)
         cudaStreamDestroy(b->cap);
+    if (b->side)
+        cudaStreamDestroy(b->side);
+    for (cudaEvent_t ev : b->ev_field)
+        cudaEventDestroy(ev);
+    b->ev_field.clear();
+    if (b->ev_fork)
+        cudaEventDestroy(b->ev_fork);
+    if (b->ev_join)
+        cudaEventDestroy(b->ev_join);
+    b->side = nullptr;
+    b->ev_fork = b->ev_join = nullptr;
     for (int q = 0; q < fb_batch::kCopyStreams; q++) {
         if (b->copy_st[q])
             cudaStreamDestroy(b->copy_st[q]);
@@ -1100,6 +1117,8 @@ int batch_build(int precision, const fb_field2d *fields, int nf, int out_f64, fb
         return fail(FB_ERR_ARG, "mixed must be 0 or 1 (got %d)", kn.mixed);
     if (kn.cols_pipe < 0 || kn.cols_pipe > 2)
         return fail(FB_ERR_ARG, "cols_pipe must be 0, 1 or 2 (got %d)", kn.cols_pipe);
+    if (kn.interleave != 0 && kn.interleave != 1)
+        return fail(FB_ERR_ARG, "interleave must be 0 or 1 (got %d)", kn.interleave);
     b->precision = precision;
     b->out_f64 = out_f64 ? 1 : 0;
     b->knobs = kn;
@@ -1351,7 +1370,7 @@ int batch_build(int precision, const fb_field2d *fields, int nf, int out_f64, fb
             // cells are evenly spaced (one tensor map over all of them)
             if (e == cudaSuccess && st.a.layout == 1 &&
                 cols_pipe_plan(precision, st.a, st.g, (int)g.f.size(), st.cp, st.pk, st.pmode,
-                               kn.cols_pipe == 0 ? -1 : (kn.cols_pipe == 1 ? 1 : 0))) {
+                               kn.interleave ? 0 : (kn.cols_pipe == 0 ? -1 : (kn.cols_pipe == 1 ? 1 : 0)))) {
                 const char *s0 = static_cast<const char *>(tp[0].src);
                 const int64_t fstride = g.f.size() > 1 ? static_cast<const char *>(tp[1].src) - s0 : 0;
                 bool even = fstride >= 0 && fstride % 16 == 0;
@@ -1373,6 +1392,22 @@ int batch_build(int precision, const fb_field2d *fields, int nf, int out_f64, fb
     e = cudaMemcpy(dv, img.data(), tables_end, cudaMemcpyHostToDevice);
     if (e != cudaSuccess)
         return cuda_fail(e, "batch tables upload");
+    // interleaved schedule: an x stage and a y stage, one field shape
+    b->interleave = kn.interleave && b->stages.size() == 2 && !b->stages[0].mixed && !b->stages[1].mixed &&
+                    b->stages[0].axis == 0 && b->stages[1].axis == 1 && b->stages[0].nf == (uint32_t)nf &&
+                    b->stages[1].nf == (uint32_t)nf;
+    if (b->interleave) {
+        e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
+        if (e == cudaSuccess)
+            e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
+        if (e == cudaSuccess)
+            e = cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming);
+        b->ev_field.assign((size_t)nf, nullptr);
+        for (int f = 0; f < nf && e == cudaSuccess; f++)
+            e = cudaEventCreateWithFlags(&b->ev_field[f], cudaEventDisableTiming);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "batch interleave streams");
+    }
     return FB_OK;
 }
 
@@ -1394,6 +1429,37 @@ int batch_enqueue(fb_batch *b, cudaStream_t st, bool prof)
         size_t e1 = prof_event(st);
         g_prof.recs.push_back({0, ev, e1});
         ev = e1;
+    }
+    if (b->interleave) {
+        // field f: x on `st`, then y on the side stream once its x is done,
+        // beside field f + 1's x; the side stream joins back at the end
+        BatchStage &sx = b->stages[0], &sy = b->stages[1];
+        const TilePtrs *tx = reinterpret_cast<const TilePtrs *>(dv + sx.off_fields);
+        const TilePtrs *ty = reinterpret_cast<const TilePtrs *>(dv + sy.off_fields);
+        e = cudaEventRecord(b->ev_fork, st);
+        if (e == cudaSuccess)
+            e = cudaStreamWaitEvent(b->side, b->ev_fork, 0);
+        for (int f = 0; f < b->nfields && e == cudaSuccess; f++) {
+            e = launch_axis_batch(1, b->precision, sx.a, sx.g, sx.sv, tx + f, sx.bpf, sx.bpf, &sx.grid, st);
+            if (e == cudaSuccess)
+                e = cudaEventRecord(b->ev_field[f], st);
+            if (e == cudaSuccess)
+                e = cudaStreamWaitEvent(b->side, b->ev_field[f], 0);
+            if (e == cudaSuccess)
+                e = launch_axis_batch(1, b->precision, sy.a, sy.g, sy.sv, ty + f, sy.bpf, sy.bpf, &sy.grid, b->side);
+        }
+        if (e == cudaSuccess)
+            e = cudaEventRecord(b->ev_join, b->side);
+        if (e == cudaSuccess)
+            e = cudaStreamWaitEvent(st, b->ev_join, 0);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "batch interleaved axis kernels");
+        if (prof) {
+            // x and y overlap: one stage (3) for both axes
+            size_t e1 = prof_event(st);
+            g_prof.recs.push_back({3, ev, e1});
+        }
+        return FB_OK;
     }
     for (size_t i = 0; i < b->stages.size(); i++) {
         BatchStage &s = b->stages[i];
@@ -1456,7 +1522,7 @@ int batch_tune(int precision, const fb_field2d *fields, int nf, int out_f64, fb_
     if (e == cudaSuccess)
         e = cudaEventCreate(&e1);
     float best_ms = 1e30f;
-    *best = fb_batch_knobs{0, 0, 0, 0};
+    *best = fb_batch_knobs{0, 0, 0, 0, 0};
     int rc = e == cudaSuccess ? FB_OK : cuda_fail(e, "tuning stream");
     // best of 5 timed runs (after 2 warm-up runs) of one candidate
     auto try_knobs = [&](fb_batch_knobs kn) {
@@ -1490,12 +1556,15 @@ int batch_tune(int precision, const fb_field2d *fields, int nf, int out_f64, fb_
     for (int c : chunks)
         for (int r : rows)
             for (int mx : mixes)
-                try_knobs(fb_batch_knobs{c, r, mx, 0});
-    // then the column kernel, both ways, on the best launch shape
+                try_knobs(fb_batch_knobs{c, r, mx, 0, 0});
+    // then the column kernel both ways, and the interleaved schedule, on the
+    // best launch shape
     const fb_batch_knobs shape = *best;
-    if (!shape.mixed)
+    if (!shape.mixed) {
         for (int pipe = 1; pipe <= 2; pipe++)
-            try_knobs(fb_batch_knobs{shape.chunk, shape.rows_threads, 0, pipe});
+            try_knobs(fb_batch_knobs{shape.chunk, shape.rows_threads, 0, pipe, 0});
+        try_knobs(fb_batch_knobs{shape.chunk, shape.rows_threads, 0, 2, 1});
+    }
     if (e0)
         cudaEventDestroy(e0);
     if (e1)

@@ -45,7 +45,7 @@ class Field2D(ctypes.Structure):
 class BatchKnobs(ctypes.Structure):
     """fb_batch_knobs: launch shape of a batch plan."""
     _fields_ = [("chunk", ctypes.c_int), ("rows_threads", ctypes.c_int), ("mixed", ctypes.c_int),
-                ("cols_pipe", ctypes.c_int)]
+                ("cols_pipe", ctypes.c_int), ("interleave", ctypes.c_int)]
 
 
 FB_BATCH_GRAPH, FB_BATCH_TUNE = 1, 2

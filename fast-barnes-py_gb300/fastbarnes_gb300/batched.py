@@ -42,9 +42,11 @@ class BatchPlan:
     out_dtype : np.float32 (default) or np.float64.
     graph     : capture the launches in a CUDA graph at the first run.
     tune      : time the candidate launch shapes at creation (runs the batch).
-    knobs     : (chunk, rows_threads[, mixed[, cols_pipe]]) to pin the launch
-                shape instead (cols_pipe: 0 library default, 1 the pipelined
-                TMA column kernel, 2 one CTA per column group).
+    knobs     : (chunk, rows_threads[, mixed[, cols_pipe[, interleave]]]) to
+                pin the launch shape instead (cols_pipe: 0 library default,
+                1 the pipelined TMA column kernel, 2 one CTA per column
+                group; interleave 1: per-field x and y launches on two
+                streams, y reading its field from L2).
     """
 
     def __init__(self, fields, *, precision='fp32c', out_dtype=np.float32, graph=True, tune=False, knobs=None,
@@ -101,8 +103,7 @@ class BatchPlan:
         flags = (_lib.FB_BATCH_GRAPH if graph else 0) | (_lib.FB_BATCH_TUNE if tune else 0)
         kn = None
         if knobs is not None:
-            kn = _lib.BatchKnobs(int(knobs[0]), int(knobs[1]), int(knobs[2]) if len(knobs) > 2 else 0,
-                                 int(knobs[3]) if len(knobs) > 3 else 0)
+            kn = _lib.BatchKnobs(*[int(knobs[q]) if len(knobs) > q else 0 for q in range(5)])
         L = _lib.lib()
         h = ctypes.c_void_p()
         with torch.cuda.device(self.device):
@@ -114,7 +115,7 @@ class BatchPlan:
     def knobs(self):
         k = _lib.BatchKnobs()
         _lib.check(_lib.lib().fb_batch_knobs_of(self._h, ctypes.byref(k)), "fb_batch_knobs_of")
-        return (k.chunk, k.rows_threads, k.mixed, k.cols_pipe)
+        return (k.chunk, k.rows_threads, k.mixed, k.cols_pipe, k.interleave)
 
     @property
     def info(self):

@@ -197,6 +197,9 @@ typedef struct fb_batch_knobs {
     int mixed;                /* 1: per-field descriptions even when the fields share one shape */
     int cols_pipe;            /* column stages: 0 library default for the precision, 1 the persistent
                                  TMA-pipelined kernel where it applies, 2 one CTA per column group */
+    int interleave;           /* 1: per-field x and y launches on two streams (field f's y right after
+                                 its x, beside field f+1's x) so that y reads an intermediate still in
+                                 L2; 0: one launch per axis for all fields */
 } fb_batch_knobs;
 
 typedef struct fb_batch fb_batch;
