@@ -12,14 +12,16 @@ of a batch plan (fb_batch_run: one sample sort and one launch per
 axis for all B fields, replayed from a CUDA graph).  `value` has the inputs
 resident in HBM; `e2e` runs the C-ABI host-buffer form
 (fb_batch_enqueue_host, two plans on two streams) from pinned host buffers,
-copies of every field's samples in and results out included.  The plain
-float64 form of the same batch, its error against the float64 result, the
-one-call-per-field entry (fb_interpolate) and the CPU oracle (the
-reference's algorithm restated in C) are reported beside it.
+copies of every field's samples in and results out included; `e2e_dropin`
+times the call a reference user makes, interpolation.barnes(numpy pts, numpy
+val, ...) -> float32 numpy, on one field.  The plain float64 form of the same
+batch, its error against the float64 result, the one-call-per-field entry
+(fb_interpolate) and the CPU oracle (the reference's algorithm restated in C)
+are reported beside it.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--batch B]
                        [--precision fp32c|fp64] [--impl gpu|reference]
-                       [--knobs CHUNK,ROWS] [--quick]
+                       [--knobs CHUNK,ROWS[,MIXED[,COLS_PIPE[,INTERLEAVE]]]] [--quick]
 For N > 1 (torchrun) every rank runs its own batch (replicas: the fields are
 independent, no collective on the data path); rank 0 prints the JSON line.
 """
@@ -362,7 +364,7 @@ def main():
     # capture of the profile summaries), scaled to B fields: the traffic
     # grows with the fields processed (independent fields, each far larger
     # than L2 once B >= 2)
-    traffic_per_field = {1: (6.503168e6 + 72.670208e6) / 2, 2: (135.293696e6 + 38.670848e6) / 2}
+    traffic_per_field = {1: (6.530048e6 + 72.707328e6) / 2, 2: (135.146496e6 + 38.249728e6) / 2}
     stage_ms = {k: statistics.median(v) for k, v in per_stage.items()}
     dom = max((k for k in stage_ms if k != 0), key=lambda k: stage_ms[k])
     peak, peak_kind = measured_peak()
