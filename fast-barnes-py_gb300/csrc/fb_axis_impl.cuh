@@ -699,6 +699,31 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
     if (kBoundsCheck && active)
         active = bounds_ok(pass_windows_in(j, K, T, E, HP, P, PP, PF, q, MODE == 1),
                            fp.hdr ? &fp.hdr->error : nullptr);
+    // The loads that nothing else waits for go first -- a columns launch's
+    // cell rows (asynchronous copies) and a splat's bin starts -- then the
+    // field's offset (thread 0) and the zeroing of the buffers run while
+    // they are in flight, and one barrier publishes it all.
+    const C *csrc = reinterpret_cast<const C *>(fp.src) + gbase;
+    const int64_t es = a.elem_stride;
+    C *dcell = cells + (size_t)HP * G;
+    if (LAYOUT == 1 && SPLAT_DIM == 0 && vec_ok) {
+        // V 16-byte asynchronous copies per row of G cells
+        constexpr int V = ColG<C>::V;
+        const int nv = V * E;
+        uint4 *d_ = reinterpret_cast<uint4 *>(dcell);
+        for (int i = tid; i < nv; i += nthr) {
+            const int row = i / V, h = i - row * V;
+            cp_async16(d_ + i, reinterpret_cast<const char *>(csrc + row * es) + 16 * h);
+        }
+    }
+    LineRanges rg;
+    rg.n = 0;
+    uint32_t total = 0;
+    __shared__ uint32_t s_tot[16];   // splat: records of each line of the CTA (at most 16 lines)
+    if (SPLAT_DIM != 0 && li < nl) {
+        rg = line_ranges<SPLAT_DIM>(line0 + li, e0, E, g, sv, fp.bin_start);
+        total = range_total(rg);
+    }
     // The field's offset and the float32 form's scalar parameters are
     // computed once per CTA: float64 instructions (including conversions to
     // float32) are scarce, and every thread needs them.
@@ -713,6 +738,31 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
         s_par[3] = (Real)a.thr;
         s_par[4] = (Real)off;
     }
+    {
+        // partial sums start at zero (their pad slots stay zero)
+        float4 *z4 = reinterpret_cast<float4 *>(part);
+        const int n4 = (int)((size_t)2 * QS * sizeof(C) / 16);
+        for (int i = tid; i < n4; i += nthr)
+            z4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    if (SPLAT_DIM != 0) {
+        // zero the line buffers
+        float4 *z4 = reinterpret_cast<float4 *>(cells);
+        const int n4 = (int)((size_t)NLC * P * sizeof(C) / 16);
+        for (int i = tid; i < n4; i += nthr)
+            z4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (li < nl && j == 0)
+            s_tot[li] = total;
+    } else if (LAYOUT == 1) {
+        // zero pad rows before and after the lines (V 16-byte vectors a row)
+        constexpr int V = ColG<C>::V;
+        uint4 *z = reinterpret_cast<uint4 *>(cells);
+        const int back = P - HP - E;
+        for (int i = tid; i < V * (HP + back); i += nthr) {
+            const int r = i / V;
+            z[V * (r < HP ? r : HP + E + (r - HP)) + (i - r * V)] = make_uint4(0u, 0u, 0u, 0u);
+        }
+    }
     __syncthreads();
     const double offset = s_offset;
     const int s0 = (int)(t0 - e0), s1 = (int)(t1 - e0);   // this tile's own cells
@@ -724,37 +774,15 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
     const bool dio = LAYOUT == 1 && SPLAT_DIM == 0 && a.passes > 0 && a.quant_bits <= 0;
 
     // ---- fill -------------------------------------------------------------
-    {
-        // partial sums start at zero (their pad slots stay zero)
-        float4 *z4 = reinterpret_cast<float4 *>(part);
-        const int n4 = (int)((size_t)2 * QS * sizeof(C) / 16);
-        for (int i = tid; i < n4; i += nthr)
-            z4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    }
     if constexpr (SPLAT_DIM != 0) {
-        // zero the line buffers, stage each line's samples with all of the
-        // line's threads, then the line's first warp adds them in order
-        float4 *z4 = reinterpret_cast<float4 *>(cells);
-        const int n4 = (int)((size_t)NLC * P * sizeof(C) / 16);
-        for (int i = tid; i < n4; i += nthr)
-            z4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        // stage each line's samples with all of the line's threads, then the
+        // line's first warp adds them in order
         StageRec<Real> *stage = reinterpret_cast<StageRec<Real> *>(part + (size_t)2 * QS);
         const SampleRec<Real> *recs = reinterpret_cast<const SampleRec<Real> *>(sv.rec);
-        __shared__ uint32_t s_rounds;
-        if (tid == 0)
-            s_rounds = 0;
-        LineRanges rg;
-        rg.n = 0;
-        uint32_t total = 0;
-        if (li < nl) {
-            rg = line_ranges<SPLAT_DIM>(line0 + li, e0, E, g, sv, fp.bin_start);
-            total = range_total(rg);
-        }
-        __syncthreads();
-        if (li < nl && j == 0)
-            atomicMax(&s_rounds, (total + kStage - 1) / kStage);
-        __syncthreads();
-        const uint32_t rounds = s_rounds;
+        uint32_t most = 0;
+        for (int q = 0; q < nl; q++)
+            most = max(most, s_tot[q]);
+        const uint32_t rounds = (most + kStage - 1) / kStage;
         StageRec<Real> *my_stage = stage + (size_t)li * kStage;
         for (uint32_t rr = 0; rr < rounds; rr++) {
             const uint32_t base = rr * kStage;
@@ -803,33 +831,12 @@ __device__ __forceinline__ void axis_tile(const AxisLaunch &a, const Geometry &g
             }
         }
     } else {
-        const C *src = reinterpret_cast<const C *>(fp.src) + gbase;
-        const int64_t es = a.elem_stride;
-        {
-            // zero pad rows before and after the lines (V 16-byte vectors a row)
-            constexpr int V = ColG<C>::V;
-            uint4 *z = reinterpret_cast<uint4 *>(cells);
-            const int back = P - HP - E;
-            for (int i = tid; i < V * (HP + back); i += nthr) {
-                const int r = i / V;
-                z[V * (r < HP ? r : HP + E + (r - HP)) + (i - r * V)] = make_uint4(0u, 0u, 0u, 0u);
-            }
-        }
-        C *dcell = cells + (size_t)HP * G;
         if (vec_ok) {
-            // V 16-byte asynchronous copies per row of G cells
-            constexpr int V = ColG<C>::V;
-            const int nv = V * E;
-            uint4 *d_ = reinterpret_cast<uint4 *>(dcell);
-            for (int i = tid; i < nv; i += nthr) {
-                const int row = i / V, h = i - row * V;
-                cp_async16(d_ + i, reinterpret_cast<const char *>(src + row * es) + 16 * h);
-            }
             cp_async_wait_all();
         } else {
             for (int i = tid; i < E * G; i += nthr) {
                 const int row = i / G, gg = i - row * G;
-                dcell[i] = gg < nl ? src[row * es + gg] : czero<C>();
+                dcell[i] = gg < nl ? csrc[row * es + gg] : czero<C>();
             }
         }
     }
