@@ -168,7 +168,7 @@ struct BatchKeyField {
     double inv_step[2];      // 1 / step (float32 form: a product instead of a division)
     int64_t size[2];
 };
-constexpr int kBatchKeysPerBlock = 512;
+constexpr int kBatchKeysPerBlock = 2048;
 // Bin-start scans of up to this many entries run as one block (one launch);
 // longer ones as tile sums, a scan of those, and tile scans (three).
 constexpr int64_t kOneBlockScanMax = 32768;

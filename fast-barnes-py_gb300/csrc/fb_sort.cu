@@ -187,19 +187,36 @@ __global__ void __launch_bounds__(1024) k_scan_exclusive(const uint32_t *__restr
 }
 
 // Places every sample into the slot of its bin that the key kernel drew; the
-// order inside a bin is fixed later.
+// order inside a bin is fixed later.  Four samples a thread, their loads
+// issued together (keys and slots, then the bin starts), so that a thread
+// waits on two round trips for all four.
+constexpr int kScatterPerThread = 4;
 __global__ void k_bin_scatter(const uint32_t *__restrict__ keys, int64_t npts, uint32_t nbins,
                               const uint32_t *__restrict__ start, const uint32_t *__restrict__ rank,
                               uint32_t *__restrict__ sorted, uint32_t *status)
 {
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < npts;
-         k += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t key = keys[k];
-        if (key < nbins) {
-            const uint32_t pos = start[key] + rank[k];
-            // bounds-check build: inside the key's bin
-            if (bounds_ok(!kBoundsCheck || pos < start[key + 1], status))
-                sorted[pos] = (uint32_t)k;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t k0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k0 < npts; k0 += kScatterPerThread * stride) {
+        uint32_t key[kScatterPerThread], rk[kScatterPerThread], st[kScatterPerThread], nx[kScatterPerThread];
+#pragma unroll
+        for (int u = 0; u < kScatterPerThread; u++) {
+            const int64_t k = k0 + u * stride;
+            key[u] = k < npts ? keys[k] : nbins;
+            rk[u] = key[u] < nbins ? rank[k] : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < kScatterPerThread; u++) {
+            st[u] = key[u] < nbins ? start[key[u]] : 0u;
+            // bounds-check build: the bin's end
+            nx[u] = kBoundsCheck && key[u] < nbins ? start[key[u] + 1] : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < kScatterPerThread; u++) {
+            if (key[u] < nbins) {
+                const uint32_t pos = st[u] + rk[u];
+                if (bounds_ok(!kBoundsCheck || pos < nx[u], status))
+                    sorted[pos] = (uint32_t)(k0 + u * stride);
+            }
         }
     }
 }
@@ -243,6 +260,29 @@ __device__ __forceinline__ void copy_rec(const uint4 *__restrict__ rec, uint4 *_
 {
     for (int w = 0; w < rw; w++)
         srec[(size_t)i * rw + w] = rec[(size_t)k * rw + w];
+}
+
+// Two record copies (the second when `two`), every load issued before the
+// first store (records of at most three words), so that the lane waits on
+// one round trip, not two.
+__device__ __forceinline__ void copy_rec2(const uint4 *__restrict__ rec, uint4 *__restrict__ srec, int rw, uint32_t k0,
+                                          uint32_t i0, bool one, uint32_t k1, uint32_t i1, bool two)
+{
+    uint4 a[3], b[3];
+#pragma unroll
+    for (int w = 0; w < 3; w++) {
+        if (one && w < rw)
+            a[w] = rec[(size_t)k0 * rw + w];
+        if (two && w < rw)
+            b[w] = rec[(size_t)k1 * rw + w];
+    }
+#pragma unroll
+    for (int w = 0; w < 3; w++) {
+        if (one && w < rw)
+            srec[(size_t)i0 * rw + w] = a[w];
+        if (two && w < rw)
+            srec[(size_t)i1 * rw + w] = b[w];
+    }
 }
 
 // Sorts one bin's entries by sample index with one warp: in registers for up
@@ -295,14 +335,12 @@ __device__ __forceinline__ bool sort_one_bin(const uint32_t *__restrict__ start,
                 }
             }
         }
-        if (lane < (int)c) {
+        const bool one = lane < (int)c, two = lane + 32 < (int)c;
+        if (one)
             sorted[s0 + lane] = x0;
-            copy_rec(rec, srec, rw, x0, s0 + lane);
-        }
-        if (lane + 32 < (int)c) {
+        if (two)
             sorted[s0 + lane + 32] = x1;
-            copy_rec(rec, srec, rw, x1, s0 + lane + 32);
-        }
+        copy_rec2(rec, srec, rw, x0, s0 + lane, one, x1, s0 + lane + 32, two);
         return true;
     }
     if (c <= kWarpSortMax) {
@@ -380,31 +418,47 @@ __global__ void __launch_bounds__(32 * kBinSortWarps) k_sort_bins(const uint32_t
 
 // Exclusive scan of counts[0, n) into bin_start by one block of 256 threads
 // (the last block of the key pass), which also clears the counts for the
-// next run.  Tiles of 1024 entries, one 16-byte load a thread, the next
-// tile's load issued before the current tile is scanned.  The counts were
-// built by device-scope atomics: read from L2.  counts must have readable
-// (ignored) entries up to n rounded up to 4.
+// next run.  Tiles of 2048 entries, 8 consecutive ones a thread (two 16-byte
+// loads, the next tile's issued before the current tile is scanned): a
+// thread sums its own entries serially, so a tile costs one warp scan and
+// three barriers.  The counts were built by device-scope atomics: read from
+// L2.  counts must have readable (ignored) entries up to n rounded up to 4.
 __device__ void last_block_scan(uint32_t *__restrict__ counts, uint32_t *__restrict__ bin_start, int64_t n)
 {
+    constexpr int E = 8, TILE = 256 * E;
     __shared__ uint32_t s_w[8];
     __shared__ uint32_t s_tot;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-    const int64_t ntile = (n + 1023) / 1024;
-    auto load = [&](int64_t tile) -> uint4 {
-        const int64_t base = tile * 1024 + 4 * t;
-        return base < n ? __ldcg(reinterpret_cast<const uint4 *>(counts + base)) : make_uint4(0u, 0u, 0u, 0u);
+    const int64_t ntile = (n + TILE - 1) / TILE;
+    uint4 cur[E / 4], nxt[E / 4];
+    auto load = [&](int64_t tile, uint4 (&v)[E / 4]) {
+#pragma unroll
+        for (int u = 0; u < E / 4; u++) {
+            const int64_t base = tile * TILE + (int64_t)E * t + 4 * u;
+            v[u] = base < n ? __ldcg(reinterpret_cast<const uint4 *>(counts + base)) : make_uint4(0u, 0u, 0u, 0u);
+        }
     };
     uint32_t carry = 0;
-    uint4 cur = load(0);
+    load(0, cur);
     for (int64_t tile = 0; tile < ntile; tile++) {
-        const uint4 nxt = tile + 1 < ntile ? load(tile + 1) : make_uint4(0u, 0u, 0u, 0u);
-        const int64_t base = tile * 1024 + 4 * t;
-        uint32_t x[4] = {cur.x, cur.y, cur.z, cur.w};
+        if (tile + 1 < ntile)
+            load(tile + 1, nxt);
+        const int64_t base = tile * TILE + (int64_t)E * t;
+        uint32_t x[E];
 #pragma unroll
-        for (int u = 0; u < 4; u++)
-            if (base + u >= n)
-                x[u] = 0u;
-        const uint32_t sum = x[0] + x[1] + x[2] + x[3];
+        for (int u = 0; u < E / 4; u++) {
+            x[4 * u] = cur[u].x;
+            x[4 * u + 1] = cur[u].y;
+            x[4 * u + 2] = cur[u].z;
+            x[4 * u + 3] = cur[u].w;
+        }
+        uint32_t sum = 0;
+#pragma unroll
+        for (int i = 0; i < E; i++) {
+            if (base + i >= n)
+                x[i] = 0u;
+            sum += x[i];
+        }
         uint32_t inc = sum;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -432,34 +486,48 @@ __device__ void last_block_scan(uint32_t *__restrict__ counts, uint32_t *__restr
         __syncthreads();
         uint32_t run = carry + s_w[w] + inc - sum;
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
-            if (base + u < n) {
-                bin_start[base + u] = run;
-                counts[base + u] = 0u;
+        for (int i = 0; i < E; i++) {
+            if (base + i < n)
+                bin_start[base + i] = run;
+            run += x[i];
+        }
+#pragma unroll
+        for (int u = 0; u < E / 4; u++) {
+            const int64_t b4 = base + 4 * u;
+            if (b4 + 3 < n) {
+                *reinterpret_cast<uint4 *>(counts + b4) = make_uint4(0u, 0u, 0u, 0u);
+            } else {
+                for (int i = 0; i < 4; i++)
+                    if (b4 + i < n)
+                        counts[b4 + i] = 0u;
             }
-            run += x[u];
         }
         carry += s_tot;
         __syncthreads();   // s_w / s_tot are rewritten by the next tile
-        cur = nxt;
+#pragma unroll
+        for (int u = 0; u < E / 4; u++)
+            cur[u] = nxt[u];
     }
 }
 
-// Bin keys and records of one block of one field's samples (256 threads, two
-// samples each, both loaded before either is worked on); keys are global
+// Bin keys and records of one block of one field's samples (256 threads,
+// kBatchKeysPerBlock / 256 samples each, taken two at a time with the next
+// two's loads issued before the current two are worked on, so that the grid
+// is about one wave and every thread has loads in flight); keys are global
 // bins (the field's bin offset + row), records indexed by global sample.
 // FUSED: the last block to finish (a ticket counter) scans the bin counts
 // into bin_start and clears the counts and the ticket for the next run, so
 // that no separate scan launch or memset is needed.
 template <typename Real, bool FUSED>
-__global__ void __launch_bounds__(256) k_batch_keys(const BatchKeyField *__restrict__ fields,
+__global__ void __launch_bounds__(256, 3) k_batch_keys(const BatchKeyField *__restrict__ fields,
                                                     const uint2 *__restrict__ blocks, uint32_t skip_key,
                                                     uint32_t *__restrict__ keys, SampleRec<Real> *__restrict__ rec,
                                                     uint32_t *__restrict__ counts, uint32_t *__restrict__ rank,
                                                     FieldHeader *__restrict__ hdrs, uint32_t *ticket,
                                                     uint32_t *__restrict__ bin_start, int64_t nscan)
 {
-    static_assert(kBatchKeysPerBlock == 512, "two samples per thread of 256");
+    constexpr int PAIRS = kBatchKeysPerBlock / 512;
+    static_assert(kBatchKeysPerBlock % 512 == 0, "pairs of samples per thread of 256");
     // Float64 instructions are few per SM on this part, so the loop keeps
     // them to the cell coordinates: the NaN test works on the bits, the
     // upper bound of the skip rule on the truncated cell index (trunc = floor
@@ -472,73 +540,97 @@ __global__ void __launch_bounds__(256) k_batch_keys(const BatchKeyField *__restr
     unsigned long long kmin = ~0ull, kmax = 0ull;
     int nan = 0;
     const int64_t end = min(f.npts, (int64_t)bt.y + kBatchKeysPerBlock);
-    int64_t ks[2];
-    double v[2], px[2], py[2];
+    // sample u of pair p: bt.y + p * 512 + u * 256 + threadIdx.x
+    double v[2][2], px[2][2], py[2][2];
+    auto load = [&](int p, int buf) {
 #pragma unroll
-    for (int u = 0; u < 2; u++) {
-        ks[u] = (int64_t)bt.y + threadIdx.x + u * 256;
-        if (ks[u] < end) {
-            v[u] = f.val[ks[u]];
-            px[u] = f.pts[2 * ks[u]];
-            py[u] = f.pts[2 * ks[u] + 1];
+        for (int u = 0; u < 2; u++) {
+            const int64_t k = (int64_t)bt.y + p * 512 + u * 256 + threadIdx.x;
+            if (k < end) {
+                v[buf][u] = f.val[k];
+                px[buf][u] = f.pts[2 * k];
+                py[buf][u] = f.pts[2 * k + 1];
+            }
+        }
+    };
+    // slots drawn by the count atomics, stored after the loop: a store
+    // right after its atomic would hold the thread on the atomic's round trip
+    uint32_t slot[PAIRS][2];
+    load(0, 0);
+#pragma unroll
+    for (int p = 0; p < PAIRS; p++) {
+        const int cb = p & 1;
+        if (p + 1 < PAIRS)
+            load(p + 1, cb ^ 1);
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const int64_t k = (int64_t)bt.y + p * 512 + u * 256 + threadIdx.x;
+            if (k >= end)
+                continue;
+            const double vu = v[cb][u];
+            const unsigned long long vb = (unsigned long long)__double_as_longlong(vu);
+            if ((vb & 0x7fffffffffffffffull) > 0x7ff0000000000000ull) {
+                nan = 1;
+            } else {
+                unsigned long long o = dbl_to_ordered(vu);
+                kmin = o < kmin ? o : kmin;
+                kmax = o > kmax ? o : kmax;
+            }
+            int xi, yi;
+            Real xw, yw;
+            bool skip;
+            if (EXACT) {
+                const double xc = (px[cb][u] - f.x0[0]) / f.step[0], yc = (py[cb][u] - f.x0[1]) / f.step[1];
+                xi = __double2int_rz(xc);
+                yi = __double2int_rz(yc);
+                skip = !(xc >= 0.0) || !(yc >= 0.0);
+                xw = (Real)(xc - (double)xi);
+                yw = (Real)(yc - (double)yi);
+            } else {
+                float xf, yf;
+                skip = !split_cell_edge(px[cb][u] - f.x0[0], f.step[0], f.inv_step[0], f.size[0], xi, xf) ||
+                       !split_cell_edge(py[cb][u] - f.x0[1], f.step[1], f.inv_step[1], f.size[1], yi, yf);
+                xw = (Real)xf;
+                yw = (Real)yf;
+            }
+            skip = skip || (int64_t)xi >= f.size[0] - 1 || (int64_t)yi >= f.size[1] - 1;
+            SampleRec<Real> r;
+            r.xi = r.yi = r.zi = 0;
+            r.xw = r.yw = r.zw = 0;
+            uint32_t key = skip_key;
+            if (!skip) {
+                r.xi = xi;
+                r.yi = yi;
+                r.xw = xw;
+                r.yw = yw;
+                key = f.bin_offset + (uint32_t)yi;
+            }
+            r.val = vu;
+            const int64_t gk = f.sample_offset + k;
+            rec[gk] = r;
+            keys[gk] = key;
+            slot[p][u] = key < skip_key ? atomicAdd(&counts[key], 1u) : ~0u;   // the sample's slot in its bin (any order)
         }
     }
 #pragma unroll
-    for (int u = 0; u < 2; u++) {
-        if (ks[u] >= end)
-            continue;
-        const int64_t k = ks[u];
-        const unsigned long long vb = (unsigned long long)__double_as_longlong(v[u]);
-        if ((vb & 0x7fffffffffffffffull) > 0x7ff0000000000000ull) {
-            nan = 1;
-        } else {
-            unsigned long long o = dbl_to_ordered(v[u]);
-            kmin = o < kmin ? o : kmin;
-            kmax = o > kmax ? o : kmax;
+    for (int p = 0; p < PAIRS; p++)
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const int64_t k = (int64_t)bt.y + p * 512 + u * 256 + threadIdx.x;
+            if (k < end && slot[p][u] != ~0u)
+                rank[f.sample_offset + k] = slot[p][u];
         }
-        int xi, yi;
-        Real xw, yw;
-        bool skip;
-        if (EXACT) {
-            const double xc = (px[u] - f.x0[0]) / f.step[0], yc = (py[u] - f.x0[1]) / f.step[1];
-            xi = __double2int_rz(xc);
-            yi = __double2int_rz(yc);
-            skip = !(xc >= 0.0) || !(yc >= 0.0);
-            xw = (Real)(xc - (double)xi);
-            yw = (Real)(yc - (double)yi);
-        } else {
-            float xf, yf;
-            skip = !split_cell_edge(px[u] - f.x0[0], f.step[0], f.inv_step[0], f.size[0], xi, xf) ||
-                   !split_cell_edge(py[u] - f.x0[1], f.step[1], f.inv_step[1], f.size[1], yi, yf);
-            xw = (Real)xf;
-            yw = (Real)yf;
-        }
-        skip = skip || (int64_t)xi >= f.size[0] - 1 || (int64_t)yi >= f.size[1] - 1;
-        SampleRec<Real> r;
-        r.xi = r.yi = r.zi = 0;
-        r.xw = r.yw = r.zw = 0;
-        uint32_t key = skip_key;
-        if (!skip) {
-            r.xi = xi;
-            r.yi = yi;
-            r.xw = xw;
-            r.yw = yw;
-            key = f.bin_offset + (uint32_t)yi;
-        }
-        r.val = v[u];
-        const int64_t gk = f.sample_offset + k;
-        rec[gk] = r;
-        keys[gk] = key;
-        if (key < skip_key)
-            rank[gk] = atomicAdd(&counts[key], 1u);   // the sample's slot in its bin (any order)
-    }
     range_to_header(kmin, kmax, nan, hdrs + bt.x);
     if constexpr (FUSED) {
+        // The block's writes are ordered before the ticket by the barrier and
+        // one release fence of the thread that takes the ticket (a fence in
+        // every thread of every block cost the pass several microseconds).
         __shared__ bool s_last;
-        __threadfence();
         __syncthreads();
-        if (threadIdx.x == 0)
+        if (threadIdx.x == 0) {
+            __threadfence();
             s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+        }
         __syncthreads();
         if (!s_last)
             return;
@@ -751,7 +843,8 @@ cudaError_t batch_sort(int precision, const BatchKeyField *d_fields, const uint2
         }
     }
     if (ntot > 0) {
-        int blocks = (int)std::min<int64_t>((ntot + 255) / 256, (int64_t)1 << 22);
+        int blocks = (int)std::min<int64_t>((ntot + 256 * kScatterPerThread - 1) / (256 * kScatterPerThread),
+                                            (int64_t)1 << 22);
         k_bin_scatter<<<blocks, 256, 0, st>>>(l.keys, ntot, nbins, bin_start, l.big, l.sorted,
                                               reinterpret_cast<uint32_t *>(&hdrs->error));
         const int rw = (int)(rec_bytes(precision) / 16);
@@ -801,7 +894,8 @@ cudaError_t sort_samples(int precision, const double *pts, const double *val, in
     }
     k_scan_exclusive<<<1, 1024, 0, st>>>(l.counts, bin_start, (int64_t)nbins + 1);
     if (npts > 0) {
-        int blocks = (int)std::min<int64_t>((npts + 255) / 256, (int64_t)1 << 22);
+        int blocks = (int)std::min<int64_t>((npts + 256 * kScatterPerThread - 1) / (256 * kScatterPerThread),
+                                            (int64_t)1 << 22);
         k_bin_scatter<<<blocks, 256, 0, st>>>(l.keys, npts, nbins, bin_start, l.big, l.sorted,
                                               reinterpret_cast<uint32_t *>(&hdr->error));
         const int rw = (int)(rec_bytes(precision) / 16);
