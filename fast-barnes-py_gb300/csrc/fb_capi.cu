@@ -228,7 +228,8 @@ int make_plan(int method, int precision, int dim, int64_t npts, const double *si
     for (int m = 0; m < dim; m++) {
         const int64_t L = size[m];
         const int T = g.T[m];
-        const AxisPlanLimits lim = axis_limits(precision, T, kchunk);
+        const int kc = m == 0 ? kchunk : axis_cols_chunk(precision, T, L, kchunk);
+        const AxisPlanLimits lim = axis_limits(precision, T, kc);
         const int64_t emax = m == 0 ? lim.extent_max : lim.extent_max_cols;
         std::vector<AxisLaunch> axl;
         AxisLaunch a{};
@@ -245,7 +246,7 @@ int make_plan(int method, int precision, int dim, int64_t npts, const double *si
         a.alpha = g.alpha[m];
         a.scaled = scaled ? 1 : 0;
         a.inv_norm = inv[m];
-        a.kchunk = kchunk;
+        a.kchunk = kc;
         a.rows_threads = rows_threads;
         bool ok = false;
         if (L <= emax) {

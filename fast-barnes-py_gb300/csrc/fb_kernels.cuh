@@ -36,6 +36,7 @@ struct AxisPlanLimits {
 };
 // Longest line extent one CTA holds for half kernel width T.
 AxisPlanLimits axis_limits(int precision, int T, int kchunk = 0);
+int axis_cols_chunk(int precision, int T, int64_t L, int kchunk);
 // Lines per columns-layout CTA: 32 bytes of (v, w) cells per grid row.
 int axis_col_group(int precision);
 // Shared memory needed by one CTA of a launch.

@@ -126,6 +126,13 @@ def interpolate(pts, val, sigma, x0, step, size, num_iter=4, max_dist=3.5,
     dim = pts.shape[1]
     val = np.ascontiguousarray(val, np.float64)
     sz = _vec(size, dim, np.int64)
+    # the reference's kernel-size check (interpolation.py:170-175, :179-184):
+    # the C restatement below assumes it and would index past its buffers
+    sg, st = _vec(sigma, dim), _vec(step, dim)
+    half = half_kernel_size_opt if method == "optimized_convolution" else half_kernel_size
+    for a in range(dim):
+        if 2 * half(sg[a], st[a], num_iter) + 1 >= sz[a]:
+            raise RuntimeError("kernel size not smaller than the grid along axis %d" % a)
     shape = tuple(int(s) for s in sz[::-1])
     out = np.empty(shape, np.float32)
     q = np.empty(shape, np.float64)

@@ -149,3 +149,18 @@ def test_smallest_grids(precision, method):
         with pytest.raises(RuntimeError):
             I.barnes(pts, val, sigma, (0.0, 0.0), step, (L - 1, L), method=method, num_iter=n,
                      precision=precision)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+@pytest.mark.parametrize("n", [1, 2, 4])
+def test_long_columns_wide_kernel(precision, n):
+    """Columns of 2048 cells with T = 94, 66, 46 (n = 1, 2, 4 at sigma = 1
+    deg, step = 75 / 4096 deg): with T > 63 the float32 y launch takes the
+    short chunk (a CTA of the long one would need more than eight warps)."""
+    rng = np.random.default_rng(40 + n)
+    step = (75.0 / 4096, 75.0 / 4096)
+    size = (192, 2048)   # at least 2T + 2 cells along x too
+    x0 = (-26.0, 34.5)
+    assert I.get_half_kernel_size_opt(1.0, step[1], n) == {1: 94, 2: 66, 4: 46}[n]
+    pts, val = edge_samples(rng, x0, step, size, 3000)
+    run_case(pts, val, 1.0, x0, step, size, n, "optimized_convolution", precision)

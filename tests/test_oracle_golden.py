@@ -151,3 +151,16 @@ def test_oracle_radius_matches_reference(golden):
         m = ~np.isnan(ref)
         assert m.any()
         assert np.max(np.abs(mine[m] - ref[m])) <= 1e-12 * np.ptp(val), ci
+
+
+def test_oracle_rejects_kernel_wider_than_grid():
+    """The reference's kernel-size check (interpolation.py:170-184) guards the
+    oracle too: a grid of at most 2T + 1 cells along an axis is refused."""
+    pts = np.array([[0.5, 0.5]])
+    val = np.array([1.0])
+    step = (75.0 / 4096, 75.0 / 4096)
+    T = oracle.half_kernel_size_opt(1.0, step[0], 1)
+    with pytest.raises(RuntimeError):
+        oracle.interpolate(pts, val, 1.0, (0.0, 0.0), step, (2 * T + 1, 2048), 1)
+    out = oracle.interpolate(pts, val, 1.0, (0.0, 0.0), step, (2 * T + 2, 2 * T + 2), 1)
+    assert out[0].shape == (2 * T + 2, 2 * T + 2)
