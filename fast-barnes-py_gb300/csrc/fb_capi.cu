@@ -16,11 +16,29 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/fastbarnes_gb300.h"
 #include "fb_internal.cuh"
 #include "fb_kernels.cuh"
 
 using namespace fbg;
+
+// NVTX range around the launches of one stage (the sample sort, one axis),
+// so that Nsight tools group and filter the kernels by stage (for example
+// ncu --nvtx --nvtx-include "fb axis 1/"); without an attached tool a push
+// or a pop costs a test of one pointer.
+struct StageRange {
+    explicit StageRange(const char *name) { nvtxRangePushA(name); }
+    ~StageRange() { nvtxRangePop(); }
+    StageRange(const StageRange &) = delete;
+    StageRange &operator=(const StageRange &) = delete;
+};
+static const char *axis_range_name(int axis)
+{
+    static const char *const names[3] = {"fb axis 0", "fb axis 1", "fb axis 2"};
+    return names[axis <= 0 ? 0 : (axis >= 2 ? 2 : axis)];
+}
 
 static thread_local char g_err[512];
 
@@ -453,8 +471,12 @@ extern "C" int fb_interpolate_grad(int method, int precision, int dim, const dou
     uint32_t *scratch = reinterpret_cast<uint32_t *>(ws + p.off_sort);
     const uint32_t *sorted = nullptr;
     const void *recs = nullptr;
-    cudaError_t e = sort_samples(p.precision, d_pts, d_val, p.npts, p.g, p.bin_w, p.nbins, hdr, scratch, bins,
-                                 &sorted, &recs, st);
+    cudaError_t e;
+    {
+        StageRange r("fb sort");
+        e = sort_samples(p.precision, d_pts, d_val, p.npts, p.g, p.bin_w, p.nbins, hdr, scratch, bins, &sorted,
+                         &recs, st);
+    }
     if (e != cudaSuccess)
         return cuda_fail(e, "sample sort");
     SampleView sv{};
@@ -475,15 +497,21 @@ extern "C" int fb_interpolate_grad(int method, int precision, int dim, const dou
         }
         AxisLaunch a = p.launches[q];
         resolve_pointers(p, ws, nullptr, a);
-        e = launch_axis(p.precision, a, p.g, sv, st);
+        {
+            StageRange r(q < gp.nfwd ? axis_range_name(a.axis) : "fb adjoint axis");
+            e = launch_axis(p.precision, a, p.g, sv, st);
+        }
         if (e != cudaSuccess)
             return cuda_fail(e, "axis kernel");
     }
     const uint32_t *keys = nullptr;
     const void *rec = nullptr;
     sort_sample_arrays(precision, p.npts, p.nbins, scratch, &keys, &rec);
-    e = launch_grad_gather(precision, dim, rec, keys, p.nbins, p.npts, ws + p.off_pair[gp.final_pair], p.g, hdr,
-                           d_grad_val, d_grad_pts, st);
+    {
+        StageRange r("fb adjoint gather");
+        e = launch_grad_gather(precision, dim, rec, keys, p.nbins, p.npts, ws + p.off_pair[gp.final_pair], p.g,
+                               hdr, d_grad_val, d_grad_pts, st);
+    }
     (void)sz;
     return e == cudaSuccess ? FB_OK : cuda_fail(e, "gradient gather");
 }
@@ -579,8 +607,12 @@ static int run_plan(Plan &p, const double *d_pts, const double *d_val, void *d_o
     uint32_t *scratch = reinterpret_cast<uint32_t *>(ws + p.off_sort);
     const uint32_t *sorted = nullptr;
     const void *recs = nullptr;
-    cudaError_t e = sort_samples(p.precision, d_pts, d_val, p.npts, p.g, p.bin_w, p.nbins, hdr, scratch, bins,
-                                 &sorted, &recs, st);
+    cudaError_t e;
+    {
+        StageRange r("fb sort");
+        e = sort_samples(p.precision, d_pts, d_val, p.npts, p.g, p.bin_w, p.nbins, hdr, scratch, bins, &sorted,
+                         &recs, st);
+    }
     if (e != cudaSuccess)
         return cuda_fail(e, "sample sort");
     if (prof) {
@@ -599,7 +631,10 @@ static int run_plan(Plan &p, const double *d_pts, const double *d_val, void *d_o
     for (AxisLaunch a : p.launches) {
         resolve_pointers(p, ws, d_out, a);
         a.out_f64 = out_f64;
-        e = launch_axis(p.precision, a, p.g, sv, st);
+        {
+            StageRange r(axis_range_name(a.axis));
+            e = launch_axis(p.precision, a, p.g, sv, st);
+        }
         if (e != cudaSuccess)
             return cuda_fail(e, "axis kernel");
         if (prof) {
@@ -1144,7 +1179,9 @@ int batch_build(int precision, const fb_field2d *fields, int nf, int out_f64, fb
         sample_off[f] = ntot;
         bin_off[f] = nbins;
         ntot += F.n_pts;
-        nbins += plans[f].nbins;
+        // the field's rows and one more bin for its skipped samples, so
+        // that its bins cover its own samples exactly
+        nbins += (int64_t)plans[f].nbins + 1;
     }
     if (ntot > (int64_t)0xFFFFFFF0ll)
         return fail(FB_ERR_ARG, "batch has too many samples (%lld)", (long long)ntot);
@@ -1297,6 +1334,16 @@ int batch_build(int precision, const fb_field2d *fields, int nf, int out_f64, fb
     }
     if (!blocks.empty())
         memcpy(img.data() + b->off_blocks, blocks.data(), sizeof(uint2) * blocks.size());
+    // bin starts: every bin of a field at the field's first sample (empty);
+    // the key pass rewrites those of fields with samples every run, those
+    // of fields without samples keep these
+    {
+        uint32_t *bs = reinterpret_cast<uint32_t *>(img.data() + b->off_bins);
+        for (int f = 0; f < nf; f++)
+            for (int64_t i = 0; i <= (int64_t)plans[f].nbins; i++)
+                bs[bin_off[f] + i] = (uint32_t)sample_off[f];
+        bs[nbins] = (uint32_t)ntot;
+    }
     const uint32_t *sorted = nullptr;
     const void *recs = nullptr;
     batch_sort_views(precision, ntot, (uint32_t)nbins, reinterpret_cast<uint32_t *>(dv + b->off_sort), &sorted,
@@ -1419,11 +1466,14 @@ int batch_enqueue(fb_batch *b, cudaStream_t st, bool prof)
     cudaError_t e;
     const uint32_t *sorted = nullptr;
     const void *recs = nullptr;
-    e = batch_sort(b->precision, reinterpret_cast<const BatchKeyField *>(dv + b->off_keyf),
-                   reinterpret_cast<const uint2 *>(dv + b->off_blocks), b->nblocks, b->ntot, b->nbins,
-                   reinterpret_cast<FieldHeader *>(dv + b->off_hdrs), b->nfields,
-                   reinterpret_cast<uint32_t *>(dv + b->off_sort), reinterpret_cast<uint32_t *>(dv + b->off_bins),
-                   &sorted, &recs, st);
+    {
+        StageRange r("fb sort");
+        e = batch_sort(b->precision, reinterpret_cast<const BatchKeyField *>(dv + b->off_keyf),
+                       reinterpret_cast<const uint2 *>(dv + b->off_blocks), b->nblocks, b->ntot, b->nbins,
+                       reinterpret_cast<FieldHeader *>(dv + b->off_hdrs), b->nfields,
+                       reinterpret_cast<uint32_t *>(dv + b->off_sort), reinterpret_cast<uint32_t *>(dv + b->off_bins),
+                       &sorted, &recs, st);
+    }
     if (e != cudaSuccess)
         return cuda_fail(e, "batch sample sort");
     if (prof) {
@@ -1441,13 +1491,18 @@ int batch_enqueue(fb_batch *b, cudaStream_t st, bool prof)
         if (e == cudaSuccess)
             e = cudaStreamWaitEvent(b->side, b->ev_fork, 0);
         for (int f = 0; f < b->nfields && e == cudaSuccess; f++) {
-            e = launch_axis_batch(1, b->precision, sx.a, sx.g, sx.sv, tx + f, sx.bpf, sx.bpf, &sx.grid, st);
+            {
+                StageRange r(axis_range_name(0));
+                e = launch_axis_batch(1, b->precision, sx.a, sx.g, sx.sv, tx + f, sx.bpf, sx.bpf, &sx.grid, st);
+            }
             if (e == cudaSuccess)
                 e = cudaEventRecord(b->ev_field[f], st);
             if (e == cudaSuccess)
                 e = cudaStreamWaitEvent(b->side, b->ev_field[f], 0);
-            if (e == cudaSuccess)
+            if (e == cudaSuccess) {
+                StageRange r(axis_range_name(1));
                 e = launch_axis_batch(1, b->precision, sy.a, sy.g, sy.sv, ty + f, sy.bpf, sy.bpf, &sy.grid, b->side);
+            }
         }
         if (e == cudaSuccess)
             e = cudaEventRecord(b->ev_join, b->side);
@@ -1464,6 +1519,7 @@ int batch_enqueue(fb_batch *b, cudaStream_t st, bool prof)
     }
     for (size_t i = 0; i < b->stages.size(); i++) {
         BatchStage &s = b->stages[i];
+        StageRange r(axis_range_name(s.axis));
         if (s.pipe)
             e = launch_cols_pipe(b->precision, s.pk, s.pmode, s.map, s.cp,
                                  reinterpret_cast<const TilePtrs *>(dv + s.off_fields), st);
@@ -1769,21 +1825,17 @@ extern "C" int fb_batch_info(const fb_batch *b, int *kernel_launches, int *memse
 {
     if (!b)
         return fail(FB_ERR_ARG, "null plan");
-    // batch_sort: k_batch_keys with the bin-start scan in its last block
-    // (fused), or k_batch_keys and a separate scan (one launch, or
-    // k_tile_sums, k_scan_exclusive and k_tile_scan for many bins) and a
-    // memset of the counts; then k_bin_scatter and k_sort_bins (which also
-    // puts the records in sorted order) when there are samples; a memset of
-    // the field headers; then one axis launch per stage with work
-    const bool fused = batch_sort_fused(b->nblocks, b->nbins);
-    const int scans = fused ? 0 : ((int64_t)b->nbins + 1 <= kOneBlockScanMax ? 1 : 3);
-    int k = scans + (b->nblocks > 0 ? 1 : 0) + (b->ntot > 0 ? 2 : 0);
+    // batch_sort: a memset of the field headers, k_batch_keys (every
+    // field's bin starts scanned by its last block) when there are samples,
+    // then k_bin_scatter and k_sort_bins (which also puts the records in
+    // sorted order); then one axis launch per stage with work
+    int k = (b->nblocks > 0 ? 1 : 0) + (b->ntot > 0 ? 2 : 0);
     for (const BatchStage &s : b->stages)
         k += s.grid > 0 ? 1 : 0;
     if (kernel_launches)
         *kernel_launches = k;
     if (memsets)
-        *memsets = fused ? 1 : 2;
+        *memsets = 1;
     if (device_bytes)
         *device_bytes = b->dev_bytes;
     return FB_OK;

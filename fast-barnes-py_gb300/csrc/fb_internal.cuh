@@ -169,9 +169,6 @@ struct BatchKeyField {
     int64_t size[2];
 };
 constexpr int kBatchKeysPerBlock = 2048;
-// Bin-start scans of up to this many entries run as one block (one launch);
-// longer ones as tile sums, a scan of those, and tile scans (three).
-constexpr int64_t kOneBlockScanMax = 32768;
 
 // Bytes of each grid row that one columns-layout CTA holds (its G adjacent
 // lines interleaved): the float32 form's and the float64 form's.

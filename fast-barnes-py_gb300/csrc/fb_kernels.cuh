@@ -11,9 +11,6 @@ cudaError_t sort_samples(int precision, const double *pts, const double *val, in
                          const uint32_t **sorted_idx, const void **recs, cudaStream_t st);
 
 size_t batch_sort_scratch_bytes(int64_t ntot, uint32_t nbins, int precision);
-// True when batch_sort runs the bin-start scan inside its key pass (one
-// launch, no counts memset): there are samples and the bins fit one block.
-bool batch_sort_fused(uint32_t nblocks, uint32_t nbins);
 // The sorted-index and record arrays batch_sort leaves in its scratch.
 void batch_sort_views(int precision, int64_t ntot, uint32_t nbins, uint32_t *scratch, const uint32_t **sorted_idx,
                       const void **recs);

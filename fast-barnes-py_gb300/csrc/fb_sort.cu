@@ -416,47 +416,41 @@ __global__ void __launch_bounds__(32 * kBinSortWarps) k_sort_bins(const uint32_t
 // batched form: the samples of many 2D fields in one set of launches
 // ---------------------------------------------------------------------------
 
-// Exclusive scan of counts[0, n) into bin_start by one block of 256 threads
-// (the last block of the key pass), which also clears the counts for the
-// next run.  Tiles of 2048 entries, 8 consecutive ones a thread (two 16-byte
-// loads, the next tile's issued before the current tile is scanned): a
-// thread sums its own entries serially, so a tile costs one warp scan and
-// three barriers.  The counts were built by device-scope atomics: read from
-// L2.  counts must have readable (ignored) entries up to n rounded up to 4.
-__device__ void last_block_scan(uint32_t *__restrict__ counts, uint32_t *__restrict__ bin_start, int64_t n)
+// Exclusive scan of counts[0, n) into bin_start (base + the scan) by one
+// block of 256 threads (the last block of a field in the key pass), which
+// also clears the counts for the next run.  Tiles of 2048 entries, 8
+// consecutive ones a thread (two 16-byte loads, the next tile's issued
+// before the current tile is scanned): a thread sums its own entries
+// serially, so a tile costs one warp scan and three barriers.  The counts
+// were built by device-scope atomics: read from L2 (plain loads, as counts
+// need not be 16-byte aligned here).
+__device__ void last_block_scan(uint32_t *__restrict__ counts, uint32_t *__restrict__ bin_start, int64_t n,
+                                uint32_t base0)
 {
     constexpr int E = 8, TILE = 256 * E;
     __shared__ uint32_t s_w[8];
     __shared__ uint32_t s_tot;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     const int64_t ntile = (n + TILE - 1) / TILE;
-    uint4 cur[E / 4], nxt[E / 4];
-    auto load = [&](int64_t tile, uint4 (&v)[E / 4]) {
+    uint32_t cur[E], nxt[E];
+    auto load = [&](int64_t tile, uint32_t (&v)[E]) {
 #pragma unroll
-        for (int u = 0; u < E / 4; u++) {
-            const int64_t base = tile * TILE + (int64_t)E * t + 4 * u;
-            v[u] = base < n ? __ldcg(reinterpret_cast<const uint4 *>(counts + base)) : make_uint4(0u, 0u, 0u, 0u);
+        for (int u = 0; u < E; u++) {
+            const int64_t i = tile * TILE + (int64_t)E * t + u;
+            v[u] = i < n ? __ldcg(counts + i) : 0u;
         }
     };
-    uint32_t carry = 0;
+    uint32_t carry = base0;
     load(0, cur);
     for (int64_t tile = 0; tile < ntile; tile++) {
         if (tile + 1 < ntile)
             load(tile + 1, nxt);
         const int64_t base = tile * TILE + (int64_t)E * t;
         uint32_t x[E];
-#pragma unroll
-        for (int u = 0; u < E / 4; u++) {
-            x[4 * u] = cur[u].x;
-            x[4 * u + 1] = cur[u].y;
-            x[4 * u + 2] = cur[u].z;
-            x[4 * u + 3] = cur[u].w;
-        }
         uint32_t sum = 0;
 #pragma unroll
         for (int i = 0; i < E; i++) {
-            if (base + i >= n)
-                x[i] = 0u;
+            x[i] = cur[i];
             sum += x[i];
         }
         uint32_t inc = sum;
@@ -492,20 +486,13 @@ __device__ void last_block_scan(uint32_t *__restrict__ counts, uint32_t *__restr
             run += x[i];
         }
 #pragma unroll
-        for (int u = 0; u < E / 4; u++) {
-            const int64_t b4 = base + 4 * u;
-            if (b4 + 3 < n) {
-                *reinterpret_cast<uint4 *>(counts + b4) = make_uint4(0u, 0u, 0u, 0u);
-            } else {
-                for (int i = 0; i < 4; i++)
-                    if (b4 + i < n)
-                        counts[b4 + i] = 0u;
-            }
-        }
+        for (int i = 0; i < E; i++)
+            if (base + i < n)
+                counts[base + i] = 0u;
         carry += s_tot;
         __syncthreads();   // s_w / s_tot are rewritten by the next tile
 #pragma unroll
-        for (int u = 0; u < E / 4; u++)
+        for (int u = 0; u < E; u++)
             cur[u] = nxt[u];
     }
 }
@@ -514,17 +501,20 @@ __device__ void last_block_scan(uint32_t *__restrict__ counts, uint32_t *__restr
 // kBatchKeysPerBlock / 256 samples each, taken two at a time with the next
 // two's loads issued before the current two are worked on, so that the grid
 // is about one wave and every thread has loads in flight); keys are global
-// bins (the field's bin offset + row), records indexed by global sample.
-// FUSED: the last block to finish (a ticket counter) scans the bin counts
-// into bin_start and clears the counts and the ticket for the next run, so
-// that no separate scan launch or memset is needed.
-template <typename Real, bool FUSED>
+// bins: the field's bin offset + row, or + H (the field's last bin, which
+// takes the samples the reference skips), so that the bins of a field cover
+// its own samples exactly and its bin starts are field-local: the last block
+// of each field to finish (a per-field ticket) scans that field's counts
+// into its bin starts (base: the field's first global sample) and clears
+// them and the ticket for the next run.  The fields' scans run side by side.
+// Records are indexed by global sample.
+template <typename Real>
 __global__ void __launch_bounds__(256, 3) k_batch_keys(const BatchKeyField *__restrict__ fields,
-                                                    const uint2 *__restrict__ blocks, uint32_t skip_key,
+                                                    const uint2 *__restrict__ blocks,
                                                     uint32_t *__restrict__ keys, SampleRec<Real> *__restrict__ rec,
                                                     uint32_t *__restrict__ counts, uint32_t *__restrict__ rank,
-                                                    FieldHeader *__restrict__ hdrs, uint32_t *ticket,
-                                                    uint32_t *__restrict__ bin_start, int64_t nscan)
+                                                    FieldHeader *__restrict__ hdrs, uint32_t *__restrict__ tickets,
+                                                    uint32_t *__restrict__ bin_start)
 {
     constexpr int PAIRS = kBatchKeysPerBlock / 512;
     static_assert(kBatchKeysPerBlock % 512 == 0, "pairs of samples per thread of 256");
@@ -597,7 +587,7 @@ __global__ void __launch_bounds__(256, 3) k_batch_keys(const BatchKeyField *__re
             SampleRec<Real> r;
             r.xi = r.yi = r.zi = 0;
             r.xw = r.yw = r.zw = 0;
-            uint32_t key = skip_key;
+            uint32_t key = f.bin_offset + (uint32_t)f.size[1];   // the field's bin of skipped samples
             if (!skip) {
                 r.xi = xi;
                 r.yi = yi;
@@ -609,7 +599,7 @@ __global__ void __launch_bounds__(256, 3) k_batch_keys(const BatchKeyField *__re
             const int64_t gk = f.sample_offset + k;
             rec[gk] = r;
             keys[gk] = key;
-            slot[p][u] = key < skip_key ? atomicAdd(&counts[key], 1u) : ~0u;   // the sample's slot in its bin (any order)
+            slot[p][u] = atomicAdd(&counts[key], 1u);   // the sample's slot in its bin (any order)
         }
     }
 #pragma unroll
@@ -617,113 +607,41 @@ __global__ void __launch_bounds__(256, 3) k_batch_keys(const BatchKeyField *__re
 #pragma unroll
         for (int u = 0; u < 2; u++) {
             const int64_t k = (int64_t)bt.y + p * 512 + u * 256 + threadIdx.x;
-            if (k < end && slot[p][u] != ~0u)
+            if (k < end)
                 rank[f.sample_offset + k] = slot[p][u];
         }
     range_to_header(kmin, kmax, nan, hdrs + bt.x);
-    if constexpr (FUSED) {
-        // The block's writes are ordered before the ticket by the barrier and
-        // one release fence of the thread that takes the ticket (a fence in
-        // every thread of every block cost the pass several microseconds).
-        __shared__ bool s_last;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            __threadfence();
-            s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
-        }
-        __syncthreads();
-        if (!s_last)
-            return;
+    // The block's writes are ordered before the ticket by the barrier and
+    // one release fence of the thread that takes the ticket.
+    __shared__ bool s_last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t nblk = (uint32_t)((f.npts + kBatchKeysPerBlock - 1) / kBatchKeysPerBlock);
         __threadfence();
-        last_block_scan(counts, bin_start, nscan);
-        if (threadIdx.x == 0)
-            *ticket = 0u;
+        s_last = atomicAdd(&tickets[bt.x], 1u) == nblk - 1;
+    }
+    __syncthreads();
+    if (!s_last)
+        return;
+    __threadfence();
+    // bins of the field: rows 0 .. H - 1 and the skipped samples' bin H; the
+    // entry after them (the next field's first) is the end of the field
+    const int64_t nb = f.size[1] + 1;
+    last_block_scan(counts + f.bin_offset, bin_start + f.bin_offset, nb, (uint32_t)f.sample_offset);
+    if (threadIdx.x == 0) {
+        bin_start[f.bin_offset + nb] = (uint32_t)(f.sample_offset + f.npts);
+        tickets[bt.x] = 0u;
     }
 }
 
-// Device-wide exclusive scan in three steps: sums of 4096-entry tiles, an
-// exclusive scan of the tile sums (one block), and every tile scanned from
-// its offset.
-__global__ void __launch_bounds__(1024) k_tile_sums(const uint32_t *__restrict__ in, int64_t n,
-                                                    uint32_t *__restrict__ sums)
-{
-    __shared__ uint32_t ws[32];
-    const int64_t base = (int64_t)blockIdx.x * 4096;
-    uint32_t s = 0;
-#pragma unroll
-    for (int u = 0; u < 4; u++) {
-        const int64_t i = base + 4 * threadIdx.x + u;
-        s += i < n ? in[i] : 0u;
-    }
-    for (int o = 16; o > 0; o >>= 1)
-        s += __shfl_xor_sync(0xffffffffu, s, o);
-    if ((threadIdx.x & 31) == 0)
-        ws[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        uint32_t t = ws[threadIdx.x];
-        for (int o = 16; o > 0; o >>= 1)
-            t += __shfl_xor_sync(0xffffffffu, t, o);
-        if (threadIdx.x == 0)
-            sums[blockIdx.x] = t;
-    }
-}
-
-__global__ void __launch_bounds__(1024) k_tile_scan(const uint32_t *__restrict__ in, int64_t n,
-                                                    const uint32_t *__restrict__ offs, uint32_t *__restrict__ out)
-{
-    __shared__ uint32_t wsum[32];
-    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-    const int64_t base = (int64_t)blockIdx.x * 4096;
-    uint32_t x[4], s = 0;
-#pragma unroll
-    for (int u = 0; u < 4; u++) {
-        const int64_t i = base + 4 * t + u;
-        x[u] = i < n ? in[i] : 0u;
-        s += x[u];
-    }
-    uint32_t inc = s;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o)
-            inc += y;
-    }
-    if (lane == 31)
-        wsum[w] = inc;
-    __syncthreads();
-    if (w == 0) {
-        const uint32_t v = wsum[lane];
-        uint32_t wi = v;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
-            if (lane >= o)
-                wi += y;
-        }
-        wsum[lane] = wi - v;
-    }
-    __syncthreads();
-    uint32_t run = offs[blockIdx.x] + wsum[w] + inc - s;
-#pragma unroll
-    for (int u = 0; u < 4; u++) {
-        const int64_t i = base + 4 * t + u;
-        if (i < n)
-            out[i] = run;
-        run += x[u];
-    }
-}
-
-
-// Scratch layout: counts[nbins + 2] | cursor[nbins + 2] (cursor[0]: the
-// batched key pass's ticket) | large[nbins + 2] (spare) |
+// Scratch layout: counts[nbins + 2] | cursor[nbins + 2] (batched form: the
+// key pass's per-field tickets) | large[nbins + 2] (spare) |
 // keys[N] | sorted[N] | big-bin scratch[2N] (uint32; its first N entries hold
 // the samples' slots in their bins until the scatter), then the sample records
-// by sample index, the records in sorted order, and (batched form) the
-// per-tile sums of the device-wide scan.
+// by sample index and the records in sorted order.
 namespace {
 struct SortLayout {
-    uint32_t *counts, *cursor, *large, *keys, *sorted, *big, *tsum;
+    uint32_t *counts, *cursor, *large, *keys, *sorted, *big;
     char *rec, *srec;
     size_t bytes;   // through the sorted records
 };
@@ -757,7 +675,6 @@ SortLayout sort_layout(uint32_t *scratch, int64_t n, uint32_t nbins, int precisi
     char *base = reinterpret_cast<char *>(scratch);
     l.rec = base + rec;
     l.srec = base + srec;
-    l.tsum = reinterpret_cast<uint32_t *>(base + end);
     l.bytes = end;
     return l;
 }
@@ -772,10 +689,9 @@ size_t sort_scratch_bytes(int64_t npts, uint32_t nbins, int precision)
 
 size_t batch_sort_scratch_bytes(int64_t ntot, uint32_t nbins, int precision)
 {
-    const size_t tiles = ((size_t)nbins + 1 + 4095) / 4096;
     size_t rec, srec, end;
     sort_offsets(ntot, nbins, precision, rec, srec, end);
-    return end + 8 * tiles + 256;
+    return end + 256;
 }
 
 void sort_sample_arrays(int precision, int64_t npts, uint32_t nbins, uint32_t *scratch, const uint32_t **keys,
@@ -799,64 +715,40 @@ cudaError_t batch_sort(int precision, const BatchKeyField *d_fields, const uint2
                        int64_t ntot, uint32_t nbins, FieldHeader *hdrs, int nfields, uint32_t *scratch,
                        uint32_t *bin_start, const uint32_t **sorted_idx, const void **recs, cudaStream_t st)
 {
+    // keys, with every field's bin starts scanned by its last block; the bin
+    // counts and the per-field tickets stay zero between runs (the key pass
+    // clears them; the plan clears them once at creation, and writes the bin
+    // starts of fields without samples, which no run touches)
     const SortLayout l = sort_layout(scratch, ntot, nbins, precision);
-    const int64_t n = (int64_t)nbins + 1;
-    // one launch for keys and bin starts when the bin starts fit one block's
-    // scan; the counts then stay zero between runs (the scanning block
-    // clears them; the plan clears them once at creation)
-    const bool fused = nblocks > 0 && n <= kOneBlockScanMax;
     cudaError_t e = cudaMemsetAsync(hdrs, 0, sizeof(FieldHeader) * (size_t)nfields, st);
-    if (e == cudaSuccess && !fused)
-        e = cudaMemsetAsync(l.counts, 0, sizeof(uint32_t) * 3 * ((size_t)nbins + 2), st);
     if (e != cudaSuccess)
         return e;
     *sorted_idx = l.sorted;
     *recs = l.srec;
-    uint32_t *ticket = l.cursor;
-#define FBG_BK(R, F)                                                                                               \
-    k_batch_keys<R, F><<<nblocks, 256, 0, st>>>(d_fields, d_blocks, nbins, l.keys,                                 \
-                                                reinterpret_cast<SampleRec<R> *>(l.rec), l.counts, l.big, hdrs,    \
-                                                ticket, bin_start, n)
     if (nblocks > 0) {
-        if (precision == 0) {
-            if (fused)
-                FBG_BK(double, true);
-            else
-                FBG_BK(double, false);
-        } else {
-            if (fused)
-                FBG_BK(float, true);
-            else
-                FBG_BK(float, false);
-        }
-    }
-#undef FBG_BK
-    if (!fused) {
-        if (n <= kOneBlockScanMax) {
-            k_scan_exclusive<<<1, 1024, 0, st>>>(l.counts, bin_start, n);
-        } else {
-            const unsigned tiles = (unsigned)((n + 4095) / 4096);
-            k_tile_sums<<<tiles, 1024, 0, st>>>(l.counts, n, l.tsum);
-            uint32_t *toff = l.tsum + tiles;
-            k_scan_exclusive<<<1, 1024, 0, st>>>(l.tsum, toff, (int64_t)tiles);
-            k_tile_scan<<<tiles, 1024, 0, st>>>(l.counts, n, toff, bin_start);
-        }
+        uint32_t *tickets = l.cursor;
+        if (precision == 0)
+            k_batch_keys<double><<<nblocks, 256, 0, st>>>(d_fields, d_blocks, l.keys,
+                                                          reinterpret_cast<SampleRec<double> *>(l.rec), l.counts,
+                                                          l.big, hdrs, tickets, bin_start);
+        else
+            k_batch_keys<float><<<nblocks, 256, 0, st>>>(d_fields, d_blocks, l.keys,
+                                                         reinterpret_cast<SampleRec<float> *>(l.rec), l.counts, l.big,
+                                                         hdrs, tickets, bin_start);
     }
     if (ntot > 0) {
+        uint32_t *status = reinterpret_cast<uint32_t *>(&hdrs->error);
         int blocks = (int)std::min<int64_t>((ntot + 256 * kScatterPerThread - 1) / (256 * kScatterPerThread),
                                             (int64_t)1 << 22);
-        k_bin_scatter<<<blocks, 256, 0, st>>>(l.keys, ntot, nbins, bin_start, l.big, l.sorted,
-                                              reinterpret_cast<uint32_t *>(&hdrs->error));
+        k_bin_scatter<<<blocks, 256, 0, st>>>(l.keys, ntot, nbins, bin_start, l.big, l.sorted, status);
         const int rw = (int)(rec_bytes(precision) / 16);
         const uint4 *rec4 = reinterpret_cast<const uint4 *>(l.rec);
         uint4 *srec4 = reinterpret_cast<uint4 *>(l.srec);
         k_sort_bins<<<(unsigned)((nbins + kBinSortWarps - 1) / kBinSortWarps), 32 * kBinSortWarps, 0, st>>>(
-            bin_start, nbins, l.sorted, rec4, srec4, rw, l.big, reinterpret_cast<uint32_t *>(&hdrs->error));
+            bin_start, nbins, l.sorted, rec4, srec4, rw, l.big, status);
     }
     return cudaGetLastError();
 }
-
-bool batch_sort_fused(uint32_t nblocks, uint32_t nbins) { return nblocks > 0 && (int64_t)nbins + 1 <= kOneBlockScanMax; }
 
 cudaError_t sort_samples(int precision, const double *pts, const double *val, int64_t npts, const Geometry &g,
                          int bin_w, uint32_t nbins, FieldHeader *hdr, uint32_t *scratch, uint32_t *bin_start,
