@@ -226,3 +226,73 @@ def test_host_buffer_batch_matches_device_run():
     assert np.array_equal(plan.outs[0].cpu().numpy(), outs[0], equal_nan=True)
     assert not np.array_equal(ref[0], outs[0], equal_nan=True)
     plan.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_batch_with_empty_and_all_skipped_fields(precision):
+    """Every field's bins cover its own range of sample slots (its rows plus
+    one bin for the samples the reference skips): fields without samples
+    (through the C ABI; the Python front door refuses them like the
+    reference's empty np.amin), a field whose samples all lie outside its
+    grid and a field with a single sample sit between ordinary ones, and
+    every field still equals its own single-field call; fields without
+    weight anywhere come out all NaN."""
+    import ctypes
+    import torch
+    from fastbarnes_gb300 import _lib
+    rng = np.random.default_rng(21)
+    specs = [
+        dict(N=3000, sigma=1.0, x0=(0.0, 0.0), step=0.05, size=(300, 200)),
+        dict(N=0, sigma=1.0, x0=(0.0, 0.0), step=0.05, size=(260, 180)),
+        dict(N=500, sigma=0.7, x0=(0.0, 0.0), step=0.05, size=(240, 160), outside=True),
+        dict(N=1, sigma=0.6, x0=(1.0, 1.0), step=0.05, size=(200, 150)),
+        dict(N=2000, sigma=0.9, x0=(-2.0, 3.0), step=0.04, size=(320, 240)),
+        dict(N=0, sigma=0.5, x0=(0.0, 0.0), step=0.05, size=(120, 100)),
+    ]
+    L = _lib.lib()
+    arr = (_lib.Field2D * len(specs))()
+    keep, host = [], []
+    for k, s in enumerate(specs):
+        size, step, x0 = np.asarray(s["size"]), s["step"], np.asarray(s["x0"])
+        if s.get("outside"):
+            pts = x0 + step * np.c_[rng.uniform(size[0] + 1, size[0] + 50, s["N"]), rng.uniform(0, size[1], s["N"])]
+        else:
+            pts = x0 + step * rng.uniform(0, size - 1, (s["N"], 2))
+        val = 20 + 5 * np.cos(pts.sum(axis=1)) + rng.normal(0, 1, s["N"])
+        tp = torch.as_tensor(pts.reshape(-1, 2), device="cuda").contiguous()
+        tv = torch.as_tensor(val, device="cuda").contiguous()
+        out = torch.empty((int(size[1]), int(size[0])), dtype=torch.float64, device="cuda")
+        keep += [tp, tv, out]
+        host.append((pts, val, s, out))
+        F = arr[k]
+        F.pts = tp.data_ptr() if s["N"] else None
+        F.val = tv.data_ptr() if s["N"] else None
+        F.n_pts = s["N"]
+        for m in range(2):
+            F.sigma[m], F.x0[m], F.step[m], F.size[m] = float(s["sigma"]), float(x0[m]), float(step), int(size[m])
+        F.num_iter = 4
+        F.max_dist_weight = np.exp(-3.5 ** 2 / 2)
+        F.method = _lib.FB_OPTIMIZED_CONVOLUTION
+        F.out = out.data_ptr()
+    prec = _lib.PRECISIONS[precision]
+    h = ctypes.c_void_p()
+    _lib.check(L.fb_batch_create(prec, arr, len(specs), 1, _lib.FB_BATCH_GRAPH, None, ctypes.byref(h)),
+               "fb_batch_create")
+    try:
+        for rep in range(2):
+            _lib.check(L.fb_batch_run(h, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)), "fb_batch_run")
+            torch.cuda.synchronize()
+            for pts, val, s, out in host:
+                o = out.cpu().numpy()
+                if s["N"] == 0 or s.get("outside"):
+                    assert np.isnan(o).all(), (s, rep)
+                    continue
+                ref = I.barnes(pts, val, s["sigma"], s["x0"], s["step"], s["size"], num_iter=4,
+                               precision=precision, out_dtype=np.float64)
+                ok, msg = same(o, ref)
+                assert ok, (s, rep, msg)
+    finally:
+        L.fb_batch_destroy(h)
+    with pytest.raises(ValueError):
+        BatchPlan([dict(pts=np.zeros((0, 2)), val=np.zeros(0), sigma=1.0, x0=(0.0, 0.0), step=0.05,
+                        size=(100, 100))])
