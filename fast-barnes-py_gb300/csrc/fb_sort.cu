@@ -363,8 +363,9 @@ __device__ __forceinline__ bool sort_one_bin(const uint32_t *__restrict__ start,
 // Sorts one bin too large for a warp with the whole block: in shared memory
 // (`sbuf`, cap entries) when it fits, else in a global scratch area of twice
 // the bin size (padded to a power of two with keys that sort last); copies
-// its records into sorted order.
-__device__ void sort_large_bin(const uint32_t *__restrict__ start, int64_t b, uint32_t *__restrict__ sorted,
+// its records into sorted order.  Not inlined: the rare path keeps its
+// registers out of the common one's (inlined, the bin sort spilled).
+__device__ __noinline__ void sort_large_bin(const uint32_t *__restrict__ start, int64_t b, uint32_t *__restrict__ sorted,
                                uint32_t *__restrict__ scratch, const uint4 *__restrict__ rec,
                                uint4 *__restrict__ srec, int rw, uint32_t *sbuf, int cap)
 {
@@ -384,32 +385,136 @@ __device__ void sort_large_bin(const uint32_t *__restrict__ start, int64_t b, ui
     __syncthreads();
 }
 
-// Sorts every bin's entries by sample index, one warp per bin
-// (sort_one_bin), so each bin lists its samples in sample order whatever
-// order the count atomics produced, and copies the records into that order.
-// A block's bins too large for a warp are then sorted by the whole block, so
-// one launch covers every bin size.
+// Bitonic network over the 64 entries of each of two bins held by one warp
+// (x[q][0]: entry lane of bin q, x[q][1]: entry lane + 32): partners 32 apart
+// sit in the same lane, the others a shuffle away; the two bins' steps are
+// independent, so their shuffles overlap.
+__device__ __forceinline__ void bitonic64_pair(uint32_t (&x)[2][2], int lane)
+{
+#pragma unroll
+    for (int k = 2; k <= 64; k <<= 1) {
+#pragma unroll
+        for (int jj = k >> 1; jj > 0; jj >>= 1) {
+            if (jj == 32) {   // k = 64: ascending everywhere
+#pragma unroll
+                for (int q = 0; q < 2; q++) {
+                    const uint32_t lo = min(x[q][0], x[q][1]), hi = max(x[q][0], x[q][1]);
+                    x[q][0] = lo;
+                    x[q][1] = hi;
+                }
+            } else {
+                const bool lower = (lane & jj) == 0;
+                const bool asc0 = (lane & k) == 0, asc1 = ((lane + 32) & k) == 0;
+                uint32_t y[2][2];
+#pragma unroll
+                for (int q = 0; q < 2; q++) {
+                    y[q][0] = __shfl_xor_sync(0xffffffffu, x[q][0], jj);
+                    y[q][1] = __shfl_xor_sync(0xffffffffu, x[q][1], jj);
+                }
+#pragma unroll
+                for (int q = 0; q < 2; q++) {
+                    x[q][0] = (lower == asc0) ? min(x[q][0], y[q][0]) : max(x[q][0], y[q][0]);
+                    x[q][1] = (lower == asc1) ? min(x[q][1], y[q][1]) : max(x[q][1], y[q][1]);
+                }
+            }
+        }
+    }
+}
+
+// Sorts every bin's entries by sample index, so each bin lists its samples
+// in sample order whatever order the count atomics produced, and copies the
+// records (RW 16-byte words each) into that order.  Each warp takes two
+// adjacent bins: their starts, entries and records are each fetched with
+// one round of loads for both, and bins of up to 64 entries are sorted in
+// registers by two interleaved bitonic networks.  A larger bin goes through
+// sort_one_bin (shared memory, up to kWarpSortMax) or, beyond that, the whole
+// block (sort_large_bin), so one launch covers every bin size.
+template <int RW>
 __global__ void __launch_bounds__(32 * kBinSortWarps) k_sort_bins(const uint32_t *__restrict__ start, uint32_t nbins,
                                                                   uint32_t *__restrict__ sorted,
                                                                   const uint4 *__restrict__ rec,
-                                                                  uint4 *__restrict__ srec, int rw,
+                                                                  uint4 *__restrict__ srec,
                                                                   uint32_t *__restrict__ scratch, uint32_t *status)
 {
     __shared__ uint32_t buf[kBinSortWarps][kWarpSortMax];
-    __shared__ int s_big[kBinSortWarps];
+    __shared__ int s_big[kBinSortWarps][2];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t b = (int64_t)blockIdx.x * kBinSortWarps + w;
-    bool done = true;
-    // bounds-check build: the bin inside the sorted arrays
-    if (b < nbins && bounds_ok(!kBoundsCheck || (start[b] <= start[b + 1] && start[b + 1] <= start[nbins]), status))
-        done = sort_one_bin(start, b, sorted, rec, srec, rw, buf[w], lane);
-    if (lane == 0)
-        s_big[w] = done ? 0 : 1;
+    const int64_t b0 = ((int64_t)blockIdx.x * kBinSortWarps + w) * 2;   // bins b0, b0 + 1
+    const int nb = (int)max((int64_t)0, min((int64_t)2, (int64_t)nbins - b0));
+    // starts of both bins and the end of the second: lanes 0 .. nb
+    const uint32_t st = lane <= nb ? start[b0 + lane] : 0u;
+    const uint32_t sa = __shfl_sync(0xffffffffu, st, 0), sb = __shfl_sync(0xffffffffu, st, 1),
+                   sc = __shfl_sync(0xffffffffu, st, 2);
+    // bounds-check build: each bin inside the sorted arrays
+    const bool ok0 = nb < 1 || bounds_ok(!kBoundsCheck || (sa <= sb && sb <= start[nbins]), status);
+    const bool ok1 = nb < 2 || bounds_ok(!kBoundsCheck || (sb <= sc && sc <= start[nbins]), status);
+    const uint32_t s0[2] = {sa, sb};
+    const int c[2] = {nb >= 1 && ok0 ? (int)(sb - sa) : 0, nb >= 2 && ok1 ? (int)(sc - sb) : 0};
+    int big[2] = {0, 0};
+    if (c[0] <= 64 && c[1] <= 64) {
+        uint32_t x[2][2];
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            x[q][0] = lane < c[q] ? sorted[s0[q] + lane] : 0xFFFFFFFFu;
+            x[q][1] = lane + 32 < c[q] ? sorted[s0[q] + lane + 32] : 0xFFFFFFFFu;
+        }
+        if (c[0] > 1 || c[1] > 1)
+            bitonic64_pair(x, lane);
+        // the records of all (up to four) entries of this lane in flight together
+        uint4 v[2][2][RW];
+#pragma unroll
+        for (int q = 0; q < 2; q++)
+#pragma unroll
+            for (int h = 0; h < 2; h++)
+                if (lane + 32 * h < c[q])
+#pragma unroll
+                    for (int u = 0; u < RW; u++)
+                        v[q][h][u] = rec[(size_t)x[q][h] * RW + u];
+#pragma unroll
+        for (int q = 0; q < 2; q++)
+#pragma unroll
+            for (int h = 0; h < 2; h++)
+                if (lane + 32 * h < c[q]) {
+                    const uint32_t pos = s0[q] + lane + 32 * h;
+                    sorted[pos] = x[q][h];
+#pragma unroll
+                    for (int u = 0; u < RW; u++)
+                        srec[(size_t)pos * RW + u] = v[q][h][u];
+                }
+    } else {
+        const bool okq[2] = {ok0, ok1};
+#pragma unroll
+        for (int q = 0; q < 2; q++)
+            if (q < nb && okq[q])
+                big[q] = sort_one_bin(start, b0 + q, sorted, rec, srec, RW, buf[w], lane) ? 0 : 1;
+    }
+    if (lane == 0) {
+        s_big[w][0] = big[0];
+        s_big[w][1] = big[1];
+    }
     __syncthreads();
     for (int q = 0; q < kBinSortWarps; q++)
-        if (s_big[q])
-            sort_large_bin(start, (int64_t)blockIdx.x * kBinSortWarps + q, sorted, scratch, rec, srec, rw,
-                           &buf[0][0], kBinSortWarps * kWarpSortMax);
+        for (int h = 0; h < 2; h++)
+            if (s_big[q][h])
+                sort_large_bin(start, ((int64_t)blockIdx.x * kBinSortWarps + q) * 2 + h, sorted, scratch, rec, srec,
+                               RW, &buf[0][0], kBinSortWarps * kWarpSortMax);
+}
+
+// Launches k_sort_bins for records of rw 16-byte words (2: float32 form, 3:
+// float64 form).
+cudaError_t launch_sort_bins(const uint32_t *start, uint32_t nbins, uint32_t *sorted, const uint4 *rec, uint4 *srec,
+                             int rw, uint32_t *scratch, uint32_t *status, cudaStream_t st)
+{
+    const unsigned grid = (unsigned)((nbins + 2 * kBinSortWarps - 1) / (2 * kBinSortWarps));
+    if (grid == 0)
+        return cudaSuccess;
+    if (rw == 2)
+        k_sort_bins<2><<<grid, 32 * kBinSortWarps, 0, st>>>(start, nbins, sorted, rec, srec, scratch, status);
+    else if (rw == 3)
+        k_sort_bins<3><<<grid, 32 * kBinSortWarps, 0, st>>>(start, nbins, sorted, rec, srec, scratch, status);
+    else
+        return cudaErrorInvalidValue;
+    return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
@@ -744,8 +849,9 @@ cudaError_t batch_sort(int precision, const BatchKeyField *d_fields, const uint2
         const int rw = (int)(rec_bytes(precision) / 16);
         const uint4 *rec4 = reinterpret_cast<const uint4 *>(l.rec);
         uint4 *srec4 = reinterpret_cast<uint4 *>(l.srec);
-        k_sort_bins<<<(unsigned)((nbins + kBinSortWarps - 1) / kBinSortWarps), 32 * kBinSortWarps, 0, st>>>(
-            bin_start, nbins, l.sorted, rec4, srec4, rw, l.big, status);
+        e = launch_sort_bins(bin_start, nbins, l.sorted, rec4, srec4, rw, l.big, status, st);
+        if (e != cudaSuccess)
+            return e;
     }
     return cudaGetLastError();
 }
@@ -793,8 +899,10 @@ cudaError_t sort_samples(int precision, const double *pts, const double *val, in
         const int rw = (int)(rec_bytes(precision) / 16);
         const uint4 *rec4 = reinterpret_cast<const uint4 *>(l.rec);
         uint4 *srec4 = reinterpret_cast<uint4 *>(l.srec);
-        k_sort_bins<<<(unsigned)((nbins + kBinSortWarps - 1) / kBinSortWarps), 32 * kBinSortWarps, 0, st>>>(
-            bin_start, nbins, l.sorted, rec4, srec4, rw, l.big, reinterpret_cast<uint32_t *>(&hdr->error));
+        e = launch_sort_bins(bin_start, nbins, l.sorted, rec4, srec4, rw, l.big,
+                             reinterpret_cast<uint32_t *>(&hdr->error), st);
+        if (e != cudaSuccess)
+            return e;
     }
     return cudaGetLastError();
 }
