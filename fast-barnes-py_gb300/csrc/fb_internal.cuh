@@ -168,6 +168,8 @@ struct BatchKeyField {
     double inv_step[2];      // 1 / step (float32 form: a product instead of a division)
     int64_t size[2];
 };
+// Samples a block of the batched key pass takes (256 threads, eight each):
+// the 800k samples of eight 100k-sample fields are about one wave of blocks.
 constexpr int kBatchKeysPerBlock = 2048;
 
 // Bytes of each grid row that one columns-layout CTA holds (its G adjacent

@@ -18,9 +18,9 @@
 
 namespace fbg {
 
-// Bin key of every sample (nbins for samples the reference skips), its cell
-// record, the count of every bin, and the min / max / NaN reduction of the
-// values.  The header and the counts start zeroed (min is kept complemented
+// Bin key of every sample (single call: nbins for samples the reference
+// skips; batched form: the field's extra bin), its cell record, the count of
+// every bin, and the min / max / NaN reduction of the values.  The header and the counts start zeroed (min is kept complemented
 // for that reason).  The float64 form divides by the step like the reference
 // (interpolation.py:247-248); the float32 form multiplies by its reciprocal.
 // Block-wide reduction of the value range (order-preserving integer keys)
