@@ -204,3 +204,41 @@ def test_radius_entry_checks_before_device_work():
     bad = (8, 8, 1000, 0.0, x0, step, size, 0.011, 0.001, 8, 1)
     assert L.fb_interpolate_radius(0, *bad, 8, 1 << 20, None) == _lib.FB_ERR_ARG
     assert b"invalid radius arguments" in L.fb_last_error()
+
+
+def test_kernel_size_guard_agrees_across_layers():
+    """The front door, the C ABI and the oracle refuse exactly the same grids
+    (interpolation.py:170-184: a grid of at most 2T + 1 cells along an axis),
+    over seeded sigma / step / n / sizes (of at least 2 cells) around the
+    limit, both methods, 2D."""
+    from oracle import oracle
+    L = _lib.lib()
+    d = _lib.dvec
+    rng = np.random.default_rng(5)
+    pts = np.asarray([[0.3, 0.4]])
+    val = np.asarray([1.0])
+    for _ in range(60):
+        method = "optimized_convolution" if rng.random() < 0.5 else "convolution"
+        helper = I.get_half_kernel_size_opt if method == "optimized_convolution" else I.get_half_kernel_size
+        n = int(rng.integers(1, 7))
+        step = float(rng.choice([0.1, 1 / 32, 0.05]))
+        sigma = float(step * rng.uniform(1.0, 8.0))
+        ks = 2 * int(helper(sigma, step, n)) + 1
+        size = (max(2, int(ks + rng.integers(-1, 2))), 2 * ks + 2)
+        refused = size[0] <= ks
+        need = ctypes.c_size_t(0)
+        rc = L.fb_workspace_size(0 if method == "optimized_convolution" else 1, 0, 2, 1, d([sigma, sigma]),
+                                 d([step, step]), d(list(size), ctypes.c_int64), n, ctypes.byref(need))
+        assert (rc == _lib.FB_ERR_KERNEL_SIZE) == refused, (method, n, sigma, step, size, rc)
+        try:
+            I._kernel_guard((ks, ks), size, 2)
+            front = False
+        except RuntimeError:
+            front = True
+        assert front == refused
+        try:
+            oracle.interpolate(pts, val, sigma, (0.0, 0.0), step, size, n, method=method)
+            orc = False
+        except RuntimeError:
+            orc = True
+        assert orc == refused, (method, n, sigma, step, size)
