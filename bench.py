@@ -364,7 +364,7 @@ def main():
     # capture of the profile summaries), scaled to B fields: the traffic
     # grows with the fields processed (independent fields, each far larger
     # than L2 once B >= 2)
-    traffic_per_field = {1: (6.530048e6 + 72.707328e6) / 2, 2: (135.146496e6 + 38.249728e6) / 2}
+    traffic_per_field = {1: (6.506752e6 + 73.150208e6) / 2, 2: (135.301120e6 + 38.189824e6) / 2}
     stage_ms = {k: statistics.median(v) for k, v in per_stage.items()}
     dom = max((k for k in stage_ms if k != 0), key=lambda k: stage_ms[k])
     peak, peak_kind = measured_peak()
